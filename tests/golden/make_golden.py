@@ -1,0 +1,441 @@
+"""Generate the golden fixtures in this folder by running the reference's own Python code.
+
+The reference (fraserac/Py-FDTD_PIC) is a flat folder of scripts.  As shipped it does not
+import: it needs numba, matplotlib and pyttsx3 (absent here) and a ``Tests`` package that does
+not exist, and ``MasterController`` runs a whole simulation at import time.  This script makes it
+runnable without changing a line of it:
+
+* ``numba`` is replaced by an inert module.  ``njit``/``jit`` return the function unchanged and
+  ``jitclass(spec)`` returns a subclass whose ``__setattr__`` applies the declared scalar type of
+  each field (``dict(spec)``: the last duplicate wins, as numba's ordered spec does).  A field
+  declared ``float32`` therefore holds the float32-rounded value, which then enters float64
+  arithmetic, exactly as reading a float32 jitclass member does inside numba.  Arrays are stored
+  by reference (no copy), as jitclass members are.
+* ``matplotlib``, ``pyttsx3`` and ``Tests.Integration_Tester`` become empty modules,
+  ``Tests.genericStability`` is the reference's own ``genericStability.py``.
+* ``MasterController.py`` is not imported; its four state classes and their specs are taken out
+  of the file with ``ast`` and executed under the jitclass stand-in.
+* ``BaseFDTD11.Nonlin_Cubic_Solver`` calls ``CubicEquationSolver.CubicSolver(a,b,c,d)`` and then
+  ``solve(CS)``; ``CubicSolver`` does not exist.  The intended callee is ``solve(a,b,c,d)``
+  (``CubicEquationSolver.py:29``), so ``CubicSolver`` packs its four arguments and ``solve``
+  unpacks them.  Nothing else in the reference is patched.
+
+Run from the repository root:  ``python tests/golden/make_golden.py`` (about two minutes).
+It reads the reference from ``/root/reference`` (or ``$PYFDTD_REFERENCE``) and writes
+``*.npz`` beside this file.  The fixtures are committed; tests only read them.
+"""
+from __future__ import annotations
+
+import ast
+import contextlib
+import importlib.util
+import io
+import os
+import sys
+import types
+import warnings
+
+import numpy as np
+import scipy
+import scipy.constants
+
+REF = os.environ.get("PYFDTD_REFERENCE", "/root/reference")
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+sys.dont_write_bytecode = True
+
+
+# ---------------------------------------------------------------------------------------------
+# inert stand-ins for the reference's missing imports
+# ---------------------------------------------------------------------------------------------
+class _NbScalar:
+    def __init__(self, name, cast):
+        self.name, self.cast = name, cast
+        self.dtype = np.dtype("bool" if name == "boolean" else name)  # usable as a numpy dtype
+
+    def __getitem__(self, idx):  # float64[:] / complex128[:, :]
+        return _NbArray(self)
+
+    def __repr__(self):
+        return self.name
+
+
+class _NbArray:
+    def __init__(self, dtype):
+        self.dtype = dtype
+
+
+def _f32(v):
+    return float(np.float32(np.real(v)))
+
+
+def _f64(v):
+    return float(np.real(v)) if np.iscomplexobj(v) else float(v)
+
+
+_TYPES = {
+    "int32": _NbScalar("int32", int),
+    "int64": _NbScalar("int64", int),
+    "float32": _NbScalar("float32", _f32),
+    "float64": _NbScalar("float64", _f64),
+    "boolean": _NbScalar("boolean", bool),
+    "complex128": _NbScalar("complex128", complex),
+}
+
+
+def _decorator_factory(*args, **kwargs):
+    if len(args) == 1 and callable(args[0]) and not kwargs:
+        return args[0]
+    return lambda f: f
+
+
+def _jitclass(spec):
+    declared = dict(spec)
+
+    def deco(cls):
+        def __setattr__(self, name, value):
+            t = declared.get(name)
+            if isinstance(t, _NbScalar):
+                value = t.cast(value)
+            object.__setattr__(self, name, value)
+
+        return type(cls.__name__, (cls,), {"__setattr__": __setattr__})
+
+    return deco
+
+
+def _install_stubs():
+    nb = types.ModuleType("numba")
+    nb.njit = nb.jit = _decorator_factory
+    nb.prange = range
+    nb.guvectorize = nb.vectorize = _decorator_factory
+    for k, v in _TYPES.items():
+        setattr(nb, k, v)
+    exp = types.ModuleType("numba.experimental")
+    exp.jitclass = _jitclass
+    nb.experimental = exp
+    typed = types.ModuleType("numba.typed")
+    typed.Dict = dict
+    nb.typed = typed
+    nbtypes = types.ModuleType("numba.types")
+    nbtypes.DictType = lambda *a: None
+    nbtypes.List = list
+    nbtypes.string = str
+    nbtypes.optional = lambda *a: None
+    nb.types = nbtypes
+    sys.modules.update({"numba": nb, "numba.experimental": exp, "numba.typed": typed,
+                        "numba.types": nbtypes})
+
+    mpl = types.ModuleType("matplotlib")
+    pylab = types.ModuleType("matplotlib.pylab")
+    pyplot = types.ModuleType("matplotlib.pyplot")
+    mpl.pylab, mpl.pyplot = pylab, pyplot
+    sys.modules.update({"matplotlib": mpl, "matplotlib.pylab": pylab, "matplotlib.pyplot": pyplot})
+    sys.modules["pyttsx3"] = types.ModuleType("pyttsx3")
+
+    tests_pkg = types.ModuleType("Tests")
+    tests_pkg.__path__ = []
+    integ = types.ModuleType("Tests.Integration_Tester")
+    integ.testerFuncVector = lambda *a, **k: {}
+    sys.modules.update({"Tests": tests_pkg, "Tests.Integration_Tester": integ})
+
+    sys.path.insert(0, REF)
+    spec = importlib.util.spec_from_file_location("Tests.genericStability",
+                                                  os.path.join(REF, "genericStability.py"))
+    gstab = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gstab)
+    sys.modules["Tests.genericStability"] = gstab
+    tests_pkg.genericStability = gstab
+
+    import CubicEquationSolver as ces  # the reference's vendored solver
+
+    raw_solve = ces.solve
+
+    def solve(*args):
+        if len(args) == 1:
+            args = tuple(args[0])
+        return raw_solve(*args)
+
+    ces.CubicSolver = lambda a, b, c, d: (a, b, c, d)
+    ces.solve = solve
+    return raw_solve
+
+
+def _load_state_classes():
+    """Execute MasterController's spec lists and four jitclasses, nothing else."""
+    src = open(os.path.join(REF, "MasterController.py")).read()
+    tree = ast.parse(src)
+    keep = []
+    for node in tree.body:
+        if isinstance(node, ast.Assign) and any(
+                isinstance(t, ast.Name) and t.id in ("specV", "specP", "specCP", "specCV")
+                for t in node.targets):
+            keep.append(node)
+        elif isinstance(node, ast.ClassDef) and node.name in (
+                "Variables", "Params", "CPML_Params", "CPML_Variables"):
+            keep.append(node)
+    mod = ast.Module(body=keep, type_ignores=[])
+    ns = {"np": np, "sci": scipy, "jclass": _jitclass}
+    ns.update(_TYPES)
+    exec(compile(mod, "MasterController.py", "exec"), ns)
+    return ns["Variables"], ns["Params"], ns["CPML_Params"], ns["CPML_Variables"]
+
+
+# ---------------------------------------------------------------------------------------------
+# cases
+# ---------------------------------------------------------------------------------------------
+C0 = 299792458.0
+
+
+def gauss_sine(n_steps, f, dt, t0=200.0, sigma=60.0, amp=1.0):
+    """Gaussian-modulated sine, the soft source of the 1000-cell workload."""
+    n = np.arange(n_steps, dtype=np.float64)
+    return amp * np.exp(-0.5 * ((n - t0) / sigma) ** 2) * np.sin(2.0 * np.pi * f * (n - t0) * dt)
+
+
+def make_params(Params, *, Nz, steps, dz, sc, front, rear, pml, nzsrc, x1, x2, freq_in):
+    dt = sc * dz / C0
+    P = Params(Nz, steps, 0, 0, 1.0, 1.0, 1.0, 1.0, x1, x2, front, rear, pml, nzsrc,
+               C0 / freq_in, dz, dt, sc, 1.0 / freq_in, 10.0, False, Nz * dz, freq_in, 20)
+    P.vidInterval = 50
+    return P
+
+
+def lorentz(V, d_eps, f0, gamma):
+    w0 = 2.0 * np.pi * f0
+    V.omega_0E = w0
+    V.plasmaFreqE = np.sqrt(d_eps) * w0
+    V.gammaE = gamma
+
+
+def run_case(mods, integrator, P, V_setup, source=None, extra_probes=(), keep_history=True):
+    Variables, Params, CPML_Params, CPML_Variables = mods["classes"]
+    SE, B11 = mods["SE"], mods["B11"]
+    V = Variables(P.Nz, P.timeSteps, P.vidInterval, 1)
+    V_setup(V)
+    C_P = CPML_Params(P.dz)
+    C_V = CPML_Variables(P.Nz, P.timeSteps)
+    pf_in = V.plasmaFreqE
+
+    trace = {c: [] for c in extra_probes}
+    orig_probe = SE.probeSim
+    orig_source = SE.SourceManager
+
+    def probe(V_, P_, C_V_, C_P_, counts, *a, **k):
+        for c in extra_probes:
+            trace[c].append(V_.Ex[c])
+        return orig_probe(V_, P_, C_V_, C_P_, counts, *a, **k)
+
+    SE.probeSim = probe
+    if source is not None:
+        SE.SourceManager = lambda V_, P_, C_V_, C_P_: (source[0].copy(), source[1].copy())
+    try:
+        with contextlib.redirect_stdout(io.StringIO()), warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            fin_be = int(P.timeSteps * 0.7)
+            st_af = int(P.timeSteps * 0.05)
+            V.x1ColBe = np.zeros(P.timeSteps)
+            V.x1ColAf = np.zeros(P.timeSteps)
+            out = getattr(SE, integrator)(V, P, C_V, C_P, fin_be, st_af)
+    finally:
+        SE.probeSim = orig_probe
+        SE.SourceManager = orig_source
+    Ex, Hy, Exs, Hys, psiE, psiH, be, af = out
+    res = dict(
+        Ex=np.asarray(Ex, float), Hy=np.asarray(Hy, float), Exs=np.asarray(Exs, float),
+        Hys=np.asarray(Hys, float), psi_Ex=np.asarray(psiE, float), psi_Hy=np.asarray(psiH, float),
+        x1ColBe=np.asarray(be, float), x1ColAf=np.asarray(af, float),
+        Dx=np.asarray(V.Dx, float), polarisationCurr=np.asarray(V.polarisationCurr, float),
+        Acubic=np.asarray(V.Acubic, float), Port1=np.asarray(V.Port1, float),
+        Port2=np.asarray(V.Port2, float), Ex_History=np.asarray(V.Ex_History, float),
+        plasmaFreqE_in=pf_in, plasmaFreqE_out=V.plasmaFreqE,
+        omega_0E=V.omega_0E, gammaE=V.gammaE, chi3Stat=V.chi3Stat, alpha3=V.alpha3,
+        beX=C_V.beX.copy(), ceX=C_V.ceX.copy(), bmY=C_V.bmY.copy(), cmY=C_V.cmY.copy(),
+        Cb=C_V.Cb.copy(), C2=C_V.C2.copy(), den_Exdz=C_V.den_Exdz.copy(),
+        den_Hydz=C_V.den_Hydz.copy(), kappaMax=C_P.kappaMax, alphaMax=C_P.alphaMax,
+        sigmaOpt=C_P.sigmaOpt, r_scale=C_P.r_scale, r_a_scale=C_P.r_a_scale,
+    )
+    for c in extra_probes:
+        res[f"probe_{c}"] = np.asarray(trace[c], float)
+    if not keep_history:
+        del res["Ex_History"]
+    scal = dict(Nz=P.Nz, timeSteps=P.timeSteps, dz=P.dz, delT=P.delT, courantNo=P.courantNo,
+                materialFrontEdge=P.materialFrontEdge, materialRearEdge=P.materialRearEdge,
+                pmlWidth=P.pmlWidth, nzsrc=P.nzsrc, x1Loc=P.x1Loc, x2Loc=P.x2Loc,
+                freq_in=P.freq_in, permit_0=P.permit_0, permea_0=P.permea_0, CharImp=P.CharImp,
+                c0=P.c0, TFSF=P.TFSF, SineCont=P.SineCont, Gaussian=P.Gaussian,
+                nonLinMed=P.nonLinMed, LorentzMed=P.LorentzMed, period=P.period,
+                Periods=P.Periods, Amplitude=P.Amplitude, vidInterval=P.vidInterval,
+                CPMLXp=P.CPMLXp, CPMLXm=P.CPMLXm, epsRe=P.epsRe, muRe=P.muRe)
+    res.update({f"P_{k}": v for k, v in scal.items()})
+    res["integrator"] = integrator
+    res["source_supplied"] = source is not None
+    return res
+
+
+def cubic_cases(raw_solve):
+    """Known answers of the reference's solve() (CubicEquationSolver.py:29-90)."""
+    rng = np.random.Generator(np.random.PCG64(20261203))
+    coeffs = [(1, -6, 11, -6), (1, -3, 3, -1), (0, 0, 2, -4), (0, 1, 0, -4), (2, 0, 0, -16),
+              (4.9e-7, 2e-3, 4, -1), (1, 0, 0, 8), (1, 1, 1, -1), (3, -2, 5, -7),
+              (1, -2, 1, -1e-9), (1, -3, 3, -1 + 1e-12), (4.9e-5, 0.0128, 21.0, -20.0),
+              (4.9e-5, -0.0128, 21.0, -20.0), (4.9e-9, 1.3e-4, 5.0, -3.0)]
+    # Kerr-like polynomials: a=(a3 chi3)^2, b=2 Re(a3 eps chi3), c=|eps|^2, d=-|D/eps0|^2
+    for _ in range(60):
+        chi3 = 10 ** rng.uniform(-4, -1)
+        a3 = float(np.float32(0.7))
+        re_eps = rng.uniform(-6, 8)
+        im_eps = rng.uniform(-2, 0)
+        d = -(10 ** rng.uniform(-6, 2))
+        coeffs.append(((a3 * chi3) ** 2, 2 * a3 * re_eps * chi3, re_eps ** 2 + im_eps ** 2, d))
+    roots_re, roots_im, n_roots, cplx = [], [], [], []
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        for co in coeffs:
+            for as_complex in (False, True):
+                args = [np.complex128(x) for x in co] if as_complex else [float(x) for x in co]
+                r = np.asarray(raw_solve(*args), dtype=complex)
+                pad = np.zeros(3, complex)
+                pad[:len(r)] = r
+                roots_re.append(pad.real)
+                roots_im.append(pad.imag)
+                n_roots.append(len(r))
+                cplx.append(as_complex)
+    co = np.repeat(np.array(coeffs, float), 2, axis=0)
+    return dict(coeffs=co, roots_re=np.array(roots_re), roots_im=np.array(roots_im),
+                n_roots=np.array(n_roots), complex_input=np.array(cplx))
+
+
+def env_cases():
+    import Environment_Setup as envDef
+    import Material_Def as matDef
+    out = {}
+    rows_in, rows_out = [], []
+    for args in [(9e9, 0.7, 7000, 8000, True), (9e9, 0.7, 7000, 8000, False),
+                 (3e9, 0.5, 400, 600, False), (5e9, 0.3, 300, 900, True),
+                 (1e10, 0.2, 1000, 1001, False)]:
+        f, dom, lo, hi, nl = args
+        with contextlib.redirect_stdout(io.StringIO()):
+            r = envDef.envSetup(f, dom, lo, hi, nonLinMed=nl)
+        rows_in.append(args)
+        rows_out.append([float(x) for x in r])
+    out["env_in"] = np.array(rows_in, float)
+    out["env_out"] = np.array(rows_out, float)
+    rows_in, rows_out = [], []
+    for args in [(3e9, 0.5, 400, 800), (1e9, 0.5, 400, 800), (2.4e9, 1.0, 500, 900)]:
+        with contextlib.redirect_stdout(io.StringIO()):
+            r = matDef.matSetup(None, None, None, None, *args)
+        rows_in.append(args)
+        rows_out.append([float(x) for x in r])
+    out["mat_in"] = np.array(rows_in, float)
+    out["mat_out"] = np.array(rows_out, float)
+    return out
+
+
+def stab_cases():
+    gstab = sys.modules["Tests.genericStability"]
+    ins, outs = [], []
+    for args in [(4096, 1000, 0.015, 1e9, 0.5 * 0.015 / C0, np.sqrt(2) * 2 * np.pi * 1.5e9,
+                  2 * np.pi * 1.5e9, 2 * np.pi * 0.1e9),
+                 (19250, 11555, 9.5172e-5, 9e9, 3.0159e-13, np.sqrt(1.5 * (2 * np.pi * 20e9) ** 2),
+                  2 * np.pi * 20e9, 2 * np.pi * 20e9 * 0.1),
+                 (8192, 4000, 0.015, 1e9, 0.5 * 0.015 / C0, np.sqrt(3.0) * 2 * np.pi * 0.9e9,
+                  2 * np.pi * 0.9e9, 2 * np.pi * 0.1e9)]:
+        with contextlib.redirect_stdout(io.StringIO()), warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            r = gstab.spatialStab(*args)
+        ins.append(args)
+        outs.append([float(np.real(x)) for x in r])
+    return dict(stab_in=np.array(ins, float), stab_out=np.array(outs, float))
+
+
+def main():
+    raw_solve = _install_stubs()
+    import BaseFDTD11 as B11
+    import Solver_Engine as SE
+    mods = dict(classes=_load_state_classes(), SE=SE, B11=B11)
+    Variables, Params, CPML_Params, CPML_Variables = mods["classes"]
+    meta = dict(numpy=np.__version__, scipy=scipy.__version__,
+                eps0=scipy.constants.epsilon_0, mu0=scipy.constants.mu_0)
+
+    np.savez_compressed(os.path.join(OUT, "cubic_solve.npz"), **cubic_cases(raw_solve), **meta)
+    np.savez_compressed(os.path.join(OUT, "setup.npz"), **env_cases(), **stab_cases(), **meta)
+
+    # 1) the 1000-cell Kerr workload: Nz=1000, dz=15 mm, Sc=0.5, 4096 steps, slab 400-599,
+    #    Lorentz eps (d_eps=2, f0=1.5 GHz, gamma=2 pi 0.1 GHz) entering the cubic, chi3=1e-2,
+    #    soft Gaussian-modulated 1 GHz source at cell 100, PML 20, extra probes at 50 and 950.
+    def cfg0(V):
+        lorentz(V, 2.0, 1.5e9, 2 * np.pi * 0.1e9)
+        V.chi3Stat = 1e-2
+
+    dz, sc, f = 0.015, 0.5, 1e9
+    P = make_params(Params, Nz=1000, steps=4096, dz=dz, sc=sc, front=400, rear=600, pml=20,
+                    nzsrc=100, x1=50, x2=950, freq_in=f)
+    P.nonLinMed, P.FreeSpace, P.TFSF = True, False, False
+    src = gauss_sine(P.timeSteps, f, P.delT)
+    r = run_case(mods, "IntegratorNL1D", P, cfg0, source=(src, np.zeros_like(src)),
+                 extra_probes=(50, 950), keep_history=False)
+    np.savez_compressed(os.path.join(OUT, "kerr_nz1000.npz"), **r, **meta)
+    print("kerr_nz1000 done", flush=True)
+
+    # 2) the same grid in the Lorentz (two-pass) integrator, probes x1Loc=50, x2Loc=950
+    P = make_params(Params, Nz=1000, steps=4096, dz=dz, sc=sc, front=400, rear=600, pml=20,
+                    nzsrc=100, x1=50, x2=950, freq_in=f)
+    P.LorentzMed, P.FreeSpace, P.TFSF = True, False, False
+    r = run_case(mods, "IntegratorLinLor1D", P, cfg0, source=(src, np.zeros_like(src)),
+                 keep_history=False)
+    np.savez_compressed(os.path.join(OUT, "lorentz_nz1000.npz"), **r, **meta)
+    print("lorentz_nz1000 done", flush=True)
+
+    # 3) the reference's own source path: SineCont with the 0.8 f pump and TF/SF, Kerr slab,
+    #    Sc=0.95 (float32), small grid
+    P = make_params(Params, Nz=600, steps=900, dz=1e-3, sc=0.95, front=300, rear=480, pml=40,
+                    nzsrc=150, x1=280, x2=60, freq_in=9e9)
+    P.nonLinMed, P.FreeSpace, P.TFSF, P.SineCont, P.Periods = True, False, True, True, 1000
+
+    def nl_default(V):
+        V.chi3Stat = 1e-3
+
+    r = run_case(mods, "IntegratorNL1D", P, nl_default)
+    np.savez_compressed(os.path.join(OUT, "kerr_sinecont_tfsf.npz"), **r, **meta)
+    print("kerr_sinecont_tfsf done", flush=True)
+
+    # 4) Lorentz two-pass with SineCont + TF/SF (the reference's sweep setting), small grid
+    P = make_params(Params, Nz=500, steps=700, dz=1e-3, sc=0.95, front=260, rear=499, pml=30,
+                    nzsrc=120, x1=240, x2=60, freq_in=9e9)
+    P.LorentzMed, P.FreeSpace, P.TFSF, P.SineCont, P.Periods = True, False, True, True, 1000
+    r = run_case(mods, "IntegratorLinLor1D", P, lambda V: None)
+    np.savez_compressed(os.path.join(OUT, "lorentz_sinecont_tfsf.npz"), **r, **meta)
+    print("lorentz_sinecont_tfsf done", flush=True)
+
+    # 5) free space (two passes, sech-modulated Gaussian source with TF/SF)
+    P = make_params(Params, Nz=400, steps=600, dz=1e-3, sc=0.95, front=250, rear=330, pml=25,
+                    nzsrc=100, x1=230, x2=50, freq_in=9e9)
+    P.FreeSpace, P.TFSF, P.Gaussian = True, True, True
+    r = run_case(mods, "IntegratorFreeSpace1D", P, lambda V: None)
+    np.savez_compressed(os.path.join(OUT, "freespace_gauss_tfsf.npz"), **r, **meta)
+    print("freespace_gauss_tfsf done", flush=True)
+
+    # 6) CPML set-up with a stretched kappa (kappaMax=3) so the den_Exdz/den_Hydz index walk
+    #    (BaseFDTD11.py:333-357) is visible; Kerr integrator, short run
+    P = make_params(Params, Nz=300, steps=200, dz=1e-3, sc=0.95, front=150, rear=220, pml=16,
+                    nzsrc=60, x1=140, x2=30, freq_in=9e9)
+    P.nonLinMed, P.FreeSpace, P.TFSF, P.SineCont = True, False, True, True
+    orig = CPML_Params.__init__
+
+    def kappa3(self, dz_):
+        orig(self, dz_)
+        self.kappaMax = 3
+        self.alphaMax = 0.02
+
+    CPML_Params.__init__ = kappa3
+    try:
+        r = run_case(mods, "IntegratorNL1D", P, nl_default)
+    finally:
+        CPML_Params.__init__ = orig
+    np.savez_compressed(os.path.join(OUT, "kerr_kappa3.npz"), **r, **meta)
+    print("kerr_kappa3 done", flush=True)
+
+
+if __name__ == "__main__":
+    main()
