@@ -1,0 +1,163 @@
+/*
+ * fdtdpic: GB300 (sm_103a) implementation of the 1D FDTD/PIC time-stepping path of
+ * fraserac/Py-FDTD_PIC.  Plain C ABI: raw device pointers, sizes, a CUDA stream, int status.
+ *
+ * Every entry point returns FDTDPIC_OK (0) or a negative FDTDPIC_ERR_* code; none throws.
+ * Pointers named d_* are caller-owned DEVICE memory (e.g. torch tensors' data_ptr()); the calls
+ * are asynchronous on the given stream unless stated.  A handle-free design: no call keeps state
+ * between calls except the per-device function attributes set on first use.
+ *
+ * Reference interfaces replaced (file:line in fraserac/Py-FDTD_PIC):
+ *   fdtd1d_run_batch / fdtd1d_run_global
+ *       the per-step loops of Solver_Engine.IntegratorNL1D (Solver_Engine.py:220-271),
+ *       IntegratorLinLor1D (:275-371, one call per pass) and IntegratorFreeSpace1D (:142-215),
+ *       i.e. BaseFDTD11.ADE_ExUpdate (BaseFDTD11.py:664), CPML_Psi_e_Update (:365),
+ *       ADE_DxUpdate (:751), AcubicFinder/Nonlin_Cubic_Solver (:803-853) with
+ *       CubicEquationSolver.solve (CubicEquationSolver.py:29), NonLinExUpdate (:859),
+ *       ADE_TempPolCurr/ADE_PolarisationCurrent_Ex (:487, :610), ADE_ExCreate (:713),
+ *       ADE_HyUpdate (:641), CPML_Psi_m_Update (:382), probeSim (Solver_Engine.py:16),
+ *       vidMake (Solver_Engine.py:57).
+ *   fdtdpic_cubic_root0
+ *       Re(CubicEquationSolver.solve(a,b,c,d)[0]) as kept by Nonlin_Cubic_Solver
+ *       (BaseFDTD11.py:838), batched.
+ */
+#ifndef FDTDPIC_H
+#define FDTDPIC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *fdtdpic_stream_t; /* == cudaStream_t */
+
+#define FDTDPIC_ABI_VERSION 1
+
+#define FDTDPIC_OK 0
+#define FDTDPIC_ERR_ARG (-1)     /* invalid argument (sizes, pointers, modes) */
+#define FDTDPIC_ERR_OOM (-2)     /* an instance does not fit the chosen path's memory */
+#define FDTDPIC_ERR_TIMEOUT (-3) /* a bounded device-side wait gave up */
+#define FDTDPIC_ERR_NUMERIC (-4) /* non-finite state detected (see status words) */
+#define FDTDPIC_ERR_CUDA (-5)    /* a CUDA runtime call failed */
+#define FDTDPIC_ERR_NODEV (-6)   /* no usable sm_103 device */
+
+#define FDTD_MODE_FREESPACE 0 /* IntegratorFreeSpace1D */
+#define FDTD_MODE_LINLOR 1    /* IntegratorLinLor1D (one pass per instance) */
+#define FDTD_MODE_KERR 2      /* IntegratorNL1D */
+
+#define FDTDPIC_F64 8 /* precision argument: FP64 state (parity path) */
+#define FDTDPIC_F32 4 /* FP32 state, FP64 near-degenerate cubic solves */
+
+/* Per-instance status bits (d_status[i]) */
+#define FDTD_STATUS_NONFINITE 1 /* Ex or Hy not finite at the end of the call */
+#define FDTD_STATUS_SKIPPED 2   /* instance larger than smem_bytes: not run */
+
+/* PML coefficient table: per instance FDTD_TAB_ROWS rows x (2*pml+1) columns of doubles.
+ * Column c <= pml is cell c; column c > pml is cell nz+1-pml+(c-pml-1). */
+#define FDTD_TAB_BEX 0
+#define FDTD_TAB_CEX 1
+#define FDTD_TAB_CB 2
+#define FDTD_TAB_BMY 3
+#define FDTD_TAB_CMY 4
+#define FDTD_TAB_C2 5
+#define FDTD_TAB_DENE 6
+#define FDTD_TAB_DENH 7
+#define FDTD_TAB_ROWS 8
+
+/* State buffer: per instance FDTD_STATE_ARRAYS arrays of nz+1 elements of the precision's type,
+ * in this order, starting at state_offset. */
+#define FDTD_ST_EX 0
+#define FDTD_ST_HY 1
+#define FDTD_ST_DX 2
+#define FDTD_ST_P 3     /* polarisationCurr */
+#define FDTD_ST_PPREV 4 /* tempVarPol (P one step back) */
+#define FDTD_ST_PSIE 5
+#define FDTD_ST_PSIH 6
+#define FDTD_ST_A 7 /* Acubic */
+#define FDTD_STATE_ARRAYS 8
+
+/* One 1D grid ("instance").  Field names follow the reference's Params/Variables. */
+typedef struct FdtdInstance {
+    int32_t nz;            /* Params.Nz; arrays have nz+1 cells */
+    int32_t n_steps;       /* Params.timeSteps (length of the source arrays) */
+    int32_t step_begin;    /* first step this call runs (0 for a fresh run) */
+    int32_t step_end;      /* one past the last step this call runs */
+    int32_t pml;           /* Params.pmlWidth */
+    int32_t cpml_lo;       /* Params.CPMLXm */
+    int32_t cpml_hi;       /* Params.CPMLXp */
+    int32_t front;         /* Params.materialFrontEdge */
+    int32_t rear;          /* Params.materialRearEdge */
+    int32_t nzsrc;         /* Params.nzsrc */
+    int32_t tfsf;          /* Params.TFSF */
+    int32_t mode;          /* FDTD_MODE_* */
+    int32_t pol_active;    /* LinLor: 1 runs the polarisation update (pass i==1) */
+    int32_t resume;        /* 1: start from the state buffer, 0: from zero fields (FieldInit) */
+    int32_t hist_interval; /* Params.vidInterval; 0 disables snapshots */
+    int32_t hist_rows;     /* rows of this instance's snapshot buffer */
+    int32_t probe_cell[2]; /* cells sampled after every step ... */
+    int32_t probe_lo[2];   /* ... for steps probe_lo <= t <= probe_hi (inclusive) */
+    int32_t probe_hi[2];
+    double ue;       /* UpExMat outside the slab (CharImp * courantNo) */
+    double ue_slab;  /* UpExMat inside [front, rear) (free space: divided by epsRe) */
+    double uh;       /* UpHyMat outside the slab ((1/CharImp) * courantNo) */
+    double uh_slab;  /* UpHyMat inside the slab */
+    double dtdz;     /* delT/dz */
+    double eps0;     /* permit_0 */
+    double sc;       /* courantNo: the source is added as Exs[t]/sc, Hys[t]/sc */
+    double pol_a, pol_b, pol_c;    /* ADE_PolarisationCurrent_Ex's A, B, C */
+    double kerr_a, kerr_b, kerr_c; /* AcubicFinder's cub, qua, one */
+    double nl_e0;    /* permit_0 * Re(sqrt(1.2)) (NonLinExUpdate) */
+    double nl_e0chi; /* permit_0 * chi3Stat */
+    int64_t pml_offset;   /* doubles into d_pml_tab */
+    int64_t src_offset;   /* doubles into d_src: Exs[n_steps] then Hys[n_steps] */
+    int64_t probe_offset; /* elements into d_probe: [n_steps][2] */
+    int64_t state_offset; /* elements into d_state: FDTD_STATE_ARRAYS x (nz+1) */
+    int64_t hist_offset;  /* elements into d_hist: [hist_rows][nz+1] */
+} FdtdInstance;
+
+/* ---- library ---------------------------------------------------------------------------- */
+int fdtdpic_abi_version(void);
+const char *fdtdpic_strerror(int code);
+/* Writes sizeof(FdtdInstance) then the byte offset of each field, in declaration order, into
+ * out[0..n); returns the number of values available.  Lets a binding verify its struct layout. */
+int fdtdpic_instance_layout(int64_t *out, int n);
+/* SM count and the dynamic shared memory (bytes) one instance needs on the resident path
+ * (0 when it does not fit); host-only, no device memory touched. */
+int fdtdpic_device_sms(int *sms);
+int64_t fdtd1d_resident_smem_bytes(const FdtdInstance *inst, int precision);
+
+/* ---- FDTD ------------------------------------------------------------------------------ */
+/* Run steps [step_begin, step_end) of n_inst instances in one launch.  Each CTA owns one
+ * instance at a time with its fields resident in shared memory and pulls the next instance
+ * index from d_queue (one int32 of caller scratch, reset by this call) in the order d_order
+ * (n_inst indices; NULL = 0..n_inst-1).  smem_bytes is the dynamic shared memory per CTA, at
+ * least the largest fdtd1d_resident_smem_bytes of the batch (an instance that needs more is
+ * skipped and flagged FDTD_STATUS_SKIPPED; above the device limit: FDTDPIC_ERR_OOM).
+ * grid_ctas <= 0 picks the
+ * occupancy-limited grid.  d_probe rows outside an instance's probe windows are not written;
+ * d_hist/d_status/d_fallbacks may be NULL.  d_fallbacks[i] counts the FP32 path's cubic solves
+ * redone in FP64. */
+int fdtd1d_run_batch(int precision, int n_inst, const FdtdInstance *d_inst, const int32_t *d_order,
+                     const double *d_pml_tab, const double *d_src, void *d_state, void *d_probe,
+                     void *d_hist, int32_t *d_queue, int32_t *d_status, int32_t *d_fallbacks,
+                     int64_t smem_bytes, int threads_per_cta, int grid_ctas,
+                     fdtdpic_stream_t stream);
+
+/* Same steps for ONE instance of any size: fields stay in d_state (global memory) and every
+ * step is two grid-wide launches (E phase, H phase).  h_inst is the host copy of d_inst[0];
+ * the call loops over steps on the host side and is asynchronous on the stream. */
+int fdtd1d_run_global(int precision, const FdtdInstance *h_inst, const FdtdInstance *d_inst,
+                      const double *d_pml_tab, const double *d_src, void *d_state, void *d_probe,
+                      void *d_hist, int32_t *d_status, int32_t *d_fallbacks,
+                      fdtdpic_stream_t stream);
+
+/* Re(roots[0]) of n cubics a*x^3+b*x^2+c*x+d with the reference's closed form, in FP64.
+ * d_coef: n x 4 doubles (a,b,c,d); d_out: n doubles. */
+int fdtdpic_cubic_root0(int n, const double *d_coef, double *d_out, fdtdpic_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FDTDPIC_H */

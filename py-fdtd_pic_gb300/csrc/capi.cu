@@ -1,0 +1,164 @@
+// C ABI of libfdtdpic.so: argument checks and dispatch to the typed launchers.
+#include <stddef.h>
+
+#include "fdtd1d_launch.cuh"
+
+namespace fdtdpic {
+
+int cuda_status(cudaError_t e)
+{
+    if (e == cudaSuccess) return FDTDPIC_OK;
+    if (e == cudaErrorMemoryAllocation) return FDTDPIC_ERR_OOM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ||
+        e == cudaErrorNoKernelImageForDevice)
+        return FDTDPIC_ERR_NODEV;
+    return FDTDPIC_ERR_CUDA;
+}
+
+int run_batch_f64(const BatchArgs<double> &a, int threads, int grid, cudaStream_t st);
+int run_batch_f32(const BatchArgs<float> &a, int threads, int grid, cudaStream_t st);
+int run_global_f64(const FdtdInstance &h, const BatchArgs<double> &a, cudaStream_t st);
+int run_global_f32(const FdtdInstance &h, const BatchArgs<float> &a, cudaStream_t st);
+int run_cubic_root0(int n, const double *coef, double *out, cudaStream_t st);
+
+static int check_instance(const FdtdInstance &I)
+{
+    if (I.nz < 2 || I.n_steps < 0 || I.step_begin < 0 || I.step_end < I.step_begin ||
+        I.step_end > I.n_steps)
+        return FDTDPIC_ERR_ARG;
+    if (I.pml < 0 || 2 * (int64_t)I.pml + 1 > (int64_t)I.nz + 1) return FDTDPIC_ERR_ARG;
+    if (I.mode < FDTD_MODE_FREESPACE || I.mode > FDTD_MODE_KERR) return FDTDPIC_ERR_ARG;
+    if (I.nzsrc < 0 || I.nzsrc > I.nz) return FDTDPIC_ERR_ARG;
+    if (I.front < 0 || I.rear < I.front || I.rear > I.nz) return FDTDPIC_ERR_ARG;
+    for (int p = 0; p < 2; ++p)
+        if (I.probe_lo[p] <= I.probe_hi[p] && (I.probe_cell[p] < 0 || I.probe_cell[p] > I.nz))
+            return FDTDPIC_ERR_ARG;
+    if (I.hist_interval < 0 || I.hist_rows < 0) return FDTDPIC_ERR_ARG;
+    if (I.sc == 0.0) return FDTDPIC_ERR_ARG;
+    return FDTDPIC_OK;
+}
+
+}  // namespace fdtdpic
+
+using namespace fdtdpic;
+
+extern "C" {
+
+int fdtdpic_abi_version(void) { return FDTDPIC_ABI_VERSION; }
+
+const char *fdtdpic_strerror(int code)
+{
+    switch (code) {
+    case FDTDPIC_OK: return "ok";
+    case FDTDPIC_ERR_ARG: return "invalid argument";
+    case FDTDPIC_ERR_OOM: return "does not fit in memory";
+    case FDTDPIC_ERR_TIMEOUT: return "device-side wait timed out";
+    case FDTDPIC_ERR_NUMERIC: return "non-finite state";
+    case FDTDPIC_ERR_CUDA: return "CUDA runtime error";
+    case FDTDPIC_ERR_NODEV: return "no usable sm_103 device";
+    default: return "unknown error";
+    }
+}
+
+int fdtdpic_instance_layout(int64_t *out, int n)
+{
+    const int64_t v[] = {
+        (int64_t)sizeof(FdtdInstance),
+        offsetof(FdtdInstance, nz), offsetof(FdtdInstance, n_steps),
+        offsetof(FdtdInstance, step_begin), offsetof(FdtdInstance, step_end),
+        offsetof(FdtdInstance, pml), offsetof(FdtdInstance, cpml_lo),
+        offsetof(FdtdInstance, cpml_hi), offsetof(FdtdInstance, front),
+        offsetof(FdtdInstance, rear), offsetof(FdtdInstance, nzsrc),
+        offsetof(FdtdInstance, tfsf), offsetof(FdtdInstance, mode),
+        offsetof(FdtdInstance, pol_active), offsetof(FdtdInstance, resume),
+        offsetof(FdtdInstance, hist_interval), offsetof(FdtdInstance, hist_rows),
+        offsetof(FdtdInstance, probe_cell), offsetof(FdtdInstance, probe_lo),
+        offsetof(FdtdInstance, probe_hi), offsetof(FdtdInstance, ue),
+        offsetof(FdtdInstance, ue_slab), offsetof(FdtdInstance, uh),
+        offsetof(FdtdInstance, uh_slab), offsetof(FdtdInstance, dtdz),
+        offsetof(FdtdInstance, eps0), offsetof(FdtdInstance, sc),
+        offsetof(FdtdInstance, pol_a), offsetof(FdtdInstance, pol_b),
+        offsetof(FdtdInstance, pol_c), offsetof(FdtdInstance, kerr_a),
+        offsetof(FdtdInstance, kerr_b), offsetof(FdtdInstance, kerr_c),
+        offsetof(FdtdInstance, nl_e0), offsetof(FdtdInstance, nl_e0chi),
+        offsetof(FdtdInstance, pml_offset), offsetof(FdtdInstance, src_offset),
+        offsetof(FdtdInstance, probe_offset), offsetof(FdtdInstance, state_offset),
+        offsetof(FdtdInstance, hist_offset)};
+    const int nv = (int)(sizeof(v) / sizeof(v[0]));
+    for (int i = 0; i < n && i < nv; ++i) out[i] = v[i];
+    return nv;
+}
+
+int fdtdpic_device_sms(int *sms)
+{
+    int dev = 0;
+    if (!sms) return FDTDPIC_ERR_ARG;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_status(e);
+    return cuda_status(cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev));
+}
+
+int64_t fdtd1d_resident_smem_bytes(const FdtdInstance *inst, int precision)
+{
+    if (!inst || (precision != FDTDPIC_F64 && precision != FDTDPIC_F32)) return 0;
+    if (check_instance(*inst) != FDTDPIC_OK) return 0;
+    const int64_t bytes = (precision == FDTDPIC_F64 ? resident_elems<double>(*inst) * 8
+                                                    : resident_elems<float>(*inst) * 4);
+    // 227 KiB is the sm_100-family opt-in maximum per CTA; the launch re-checks the device.
+    return bytes <= 227 * 1024 ? bytes : 0;
+}
+
+int fdtd1d_run_batch(int precision, int n_inst, const FdtdInstance *d_inst, const int32_t *d_order,
+                     const double *d_pml_tab, const double *d_src, void *d_state, void *d_probe,
+                     void *d_hist, int32_t *d_queue, int32_t *d_status, int32_t *d_fallbacks,
+                     int64_t smem_bytes, int threads_per_cta, int grid_ctas,
+                     fdtdpic_stream_t stream)
+{
+    if (n_inst <= 0) return n_inst == 0 ? FDTDPIC_OK : FDTDPIC_ERR_ARG;
+    if (!d_inst || !d_pml_tab || !d_src || !d_state || !d_probe || !d_queue)
+        return FDTDPIC_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (precision == FDTDPIC_F64) {
+        BatchArgs<double> a{n_inst, d_inst, d_order, d_pml_tab, d_src, (double *)d_state,
+                            (double *)d_probe, (double *)d_hist, d_queue, d_status, d_fallbacks,
+                            smem_bytes};
+        return run_batch_f64(a, threads_per_cta, grid_ctas, st);
+    }
+    if (precision == FDTDPIC_F32) {
+        BatchArgs<float> a{n_inst, d_inst, d_order, d_pml_tab, d_src, (float *)d_state,
+                           (float *)d_probe, (float *)d_hist, d_queue, d_status, d_fallbacks,
+                           smem_bytes};
+        return run_batch_f32(a, threads_per_cta, grid_ctas, st);
+    }
+    return FDTDPIC_ERR_ARG;
+}
+
+int fdtd1d_run_global(int precision, const FdtdInstance *h_inst, const FdtdInstance *d_inst,
+                      const double *d_pml_tab, const double *d_src, void *d_state, void *d_probe,
+                      void *d_hist, int32_t *d_status, int32_t *d_fallbacks,
+                      fdtdpic_stream_t stream)
+{
+    if (!h_inst || !d_inst || !d_pml_tab || !d_src || !d_state || !d_probe) return FDTDPIC_ERR_ARG;
+    int rc = check_instance(*h_inst);
+    if (rc != FDTDPIC_OK) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (precision == FDTDPIC_F64) {
+        BatchArgs<double> a{1, d_inst, nullptr, d_pml_tab, d_src, (double *)d_state,
+                            (double *)d_probe, (double *)d_hist, nullptr, d_status, d_fallbacks, 0};
+        return run_global_f64(*h_inst, a, st);
+    }
+    if (precision == FDTDPIC_F32) {
+        BatchArgs<float> a{1, d_inst, nullptr, d_pml_tab, d_src, (float *)d_state,
+                           (float *)d_probe, (float *)d_hist, nullptr, d_status, d_fallbacks, 0};
+        return run_global_f32(*h_inst, a, st);
+    }
+    return FDTDPIC_ERR_ARG;
+}
+
+int fdtdpic_cubic_root0(int n, const double *d_coef, double *d_out, fdtdpic_stream_t stream)
+{
+    if (n < 0 || (n > 0 && (!d_coef || !d_out))) return FDTDPIC_ERR_ARG;
+    return run_cubic_root0(n, d_coef, d_out, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,435 @@
+// 1D FDTD time stepping for one grid ("instance"), templated on the state type T.
+//
+// Step order (one step t), exactly the reference's (Solver_Engine.py:236-267 for the Kerr
+// integrator, :294-370 for the Lorentz one, :167-211 for free space):
+//   E phase (cell-local given the old Hy):
+//     [LinLor, pol_active] P <- A*P + B*P_prev + C*Ex          ADE_PolarisationCurrent_Ex :610
+//     Ex <- Ex + (Hy[k]-Hy[k-1]-Jx)*UpExMat*den_Exdz            ADE_ExUpdate :664
+//     PML: psi_e <- beX*psi_e + ceX*dHy ; Ex <- Ex - Cb*psi_e     CPML_Psi_e_Update :365
+//     Ex[nzsrc] += Exs[t]/Sc ; TF/SF: Hy[nzsrc-1] -= Hys[t]/Sc   Solver_Engine.py:249-252
+//     slab: Dx <- Dx + dHy'*(dt/dz)*den_Exdz  (dHy' sees the TF/SF-corrected Hy)  :751
+//       Kerr:   A = roots[0] of cub A^3 + qua A^2 + one A - |Dx/eps0|^2 (0 if |d|<=1e-8)
+//               Ex = Dx/(eps0 Re(sqrt 1.2) + eps0 chi3 A)          :803-877
+//       LinLor: Ex = (Dx - P)/eps0                                 ADE_ExCreate :713
+//   H phase (cell-local given the new Ex):
+//     Hy <- Hy + (Ex[k+1]-Ex[k])*UpHyMat*den_Hydz                 ADE_HyUpdate :641
+//     PML: psi_h <- bmY*psi_h + cmY*dEx ; Hy <- Hy + C2*psi_h      CPML_Psi_m_Update :382
+//     snapshot (vidMake) and probes (probeSim) read the final Ex of the step.
+// Index ranges: Ex over [1, nz], Hy over [1, nz-1], psi_e over [1,pml) U [nz+1-pml, nz],
+// psi_h over [1,pml) U [nz+1-pml, nz-1], slab [front, rear).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/fdtdpic.h"
+#include "cubic.cuh"
+
+namespace fdtdpic {
+
+template <typename T>
+struct Scal {
+    T ue, ue_slab, uh, uh_slab, dtdz, eps0, pa, pb, pc, e0r, e0chi;
+};
+
+template <typename T>
+__device__ inline Scal<T> make_scal(const FdtdInstance &I)
+{
+    Scal<T> s;
+    s.ue = (T)I.ue; s.ue_slab = (T)I.ue_slab; s.uh = (T)I.uh; s.uh_slab = (T)I.uh_slab;
+    s.dtdz = (T)I.dtdz; s.eps0 = (T)I.eps0; s.pa = (T)I.pol_a; s.pb = (T)I.pol_b;
+    s.pc = (T)I.pol_c; s.e0r = (T)I.nl_e0; s.e0chi = (T)I.nl_e0chi;
+    return s;
+}
+
+// PML table column of cell k, or -1.
+__device__ __forceinline__ int pml_col(const FdtdInstance &I, int k)
+{
+    if (k <= I.pml) return k;
+    const int r0 = I.nz + 1 - I.pml;
+    if (k >= r0) return I.pml + 1 + (k - r0);
+    return -1;
+}
+
+// Kerr root in the state precision.
+template <typename T>
+struct Kerr;
+template <>
+struct Kerr<double> {
+    double a, b, c;
+    __device__ void setup(const FdtdInstance &I) { a = I.kerr_a; b = I.kerr_b; c = I.kerr_c; }
+    __device__ double root(double dx, double eps0, int *nfb) const
+    {
+        const double q = fabs(dx / eps0);
+        const double d = -(q * q);
+        return (fabs(d) > 1e-8) ? cubic_root0_f64(a, b, c, d) : 0.0;
+    }
+};
+template <>
+struct Kerr<float> {
+    KerrF32 k;
+    __device__ void setup(const FdtdInstance &I) { k = kerr_f32_setup(I.kerr_a, I.kerr_b, I.kerr_c); }
+    __device__ float root(float dx, float eps0, int *nfb) const
+    {
+        const float q = dx / eps0;
+        const float d = -(q * q);
+        return (fabsf(d) > 1e-8f) ? cubic_root0_f32(k, d, nfb) : 0.f;
+    }
+};
+
+// ---------------------------------------------------------------------------------------
+// storage back ends: shared-memory resident (compact) and global (full-length arrays)
+// ---------------------------------------------------------------------------------------
+template <typename T>
+struct SmemStore {
+    T *ex, *hy, *dx, *p, *pp, *psie, *psih, *tab;
+    int front, W;
+    __device__ T &Ex(int k) { return ex[k]; }
+    __device__ T &Hy(int k) { return hy[k]; }
+    __device__ T &Dx(int k) { return dx[k - front]; }
+    __device__ T &P(int k) { return p[k - front]; }
+    __device__ T &Pp(int k) { return pp[k - front]; }
+    __device__ T &PsiE(int col, int) { return psie[col]; }
+    __device__ T &PsiH(int col, int) { return psih[col]; }
+    __device__ T tab_at(int row, int col) const { return tab[row * W + col]; }
+};
+
+template <typename T>
+struct GlobalStore {
+    T *ex, *hy, *dx, *p, *pp, *psie, *psih;
+    const double *tab;
+    int W;
+    __device__ T &Ex(int k) { return ex[k]; }
+    __device__ T &Hy(int k) { return hy[k]; }
+    __device__ T &Dx(int k) { return dx[k]; }
+    __device__ T &P(int k) { return p[k]; }
+    __device__ T &Pp(int k) { return pp[k]; }
+    __device__ T &PsiE(int, int k) { return psie[k]; }
+    __device__ T &PsiH(int, int k) { return psih[k]; }
+    __device__ T tab_at(int row, int col) const { return (T)tab[row * W + col]; }
+};
+
+// E phase for cell k in [1, nz].  src_e = Exs[t]/Sc, src_h = Hys[t]/Sc in T.
+template <typename T, class S>
+__device__ __forceinline__ void e_cell(const FdtdInstance &I, const Scal<T> &c, const Kerr<T> &kr,
+                                       S &s, int k, T src_e, T src_h, const T *jx, T *a_out,
+                                       int *nfb)
+{
+    const int n = I.nz + 1;
+    const T hk = s.Hy(k), hkm = s.Hy(k - 1);
+    T ex = s.Ex(k);
+    const bool slab = (k >= I.front) && (k < I.rear);
+    if (I.mode == FDTD_MODE_LINLOR && I.pol_active && slab) {
+        const T pm2 = s.Pp(k);
+        const T pcur = s.P(k);
+        s.Pp(k) = pcur;
+        s.P(k) = c.pa * pcur + c.pb * pm2 + c.pc * ex;
+    }
+    const int col = pml_col(I, k);
+    const T den = (col >= 0) ? s.tab_at(FDTD_TAB_DENE, col) : T(1);
+    const T up = (I.mode == FDTD_MODE_FREESPACE && slab) ? c.ue_slab : c.ue;
+    T dh = hk - hkm;
+    if (jx) dh = dh - jx[k];
+    ex = ex + dh * up * den;
+    if ((I.cpml_lo && k < I.pml) || (I.cpml_hi && k >= n - I.pml)) {
+        T &psi = s.PsiE(col, k);
+        psi = s.tab_at(FDTD_TAB_BEX, col) * psi + s.tab_at(FDTD_TAB_CEX, col) * (hk - hkm);
+        ex = ex - s.tab_at(FDTD_TAB_CB, col) * psi;
+    }
+    if (k == I.nzsrc) ex += src_e;
+    if (I.mode != FDTD_MODE_FREESPACE && slab) {
+        T hk_d = hk, hkm_d = hkm;
+        if (I.tfsf) {
+            if (k == I.nzsrc - 1) hk_d = hk - src_h;
+            if (k == I.nzsrc) hkm_d = hkm - src_h;
+        }
+        const T dx = s.Dx(k) + (hk_d - hkm_d) * c.dtdz * den;
+        s.Dx(k) = dx;
+        if (I.mode == FDTD_MODE_KERR) {
+            const T A = kr.root(dx, c.eps0, nfb);
+            if (a_out) a_out[k] = A;
+            ex = dx / (c.e0r + c.e0chi * A);
+        } else {
+            ex = (dx - s.P(k)) / (c.eps0);
+        }
+    }
+    s.Ex(k) = ex;
+}
+
+// H phase for cell k in [1, nz-1].
+template <typename T, class S>
+__device__ __forceinline__ void h_cell(const FdtdInstance &I, const Scal<T> &c, S &s, int k,
+                                       T src_h)
+{
+    const int n = I.nz + 1;
+    T hy = s.Hy(k);
+    if (I.tfsf && k == I.nzsrc - 1) hy = hy - src_h;
+    const T exk = s.Ex(k), exk1 = s.Ex(k + 1);
+    const bool slab = (k >= I.front) && (k < I.rear);
+    const int col = pml_col(I, k);
+    const T den = (col >= 0) ? s.tab_at(FDTD_TAB_DENH, col) : T(1);
+    const T uh = (I.mode == FDTD_MODE_FREESPACE && slab) ? c.uh_slab : c.uh;
+    hy = hy + (exk1 - exk) * uh * den;
+    if ((I.cpml_lo && k < I.pml) || (I.cpml_hi && k >= n - I.pml && k < n - 1)) {
+        T &psi = s.PsiH(col, k);
+        psi = s.tab_at(FDTD_TAB_BMY, col) * psi + s.tab_at(FDTD_TAB_CMY, col) * (exk1 - exk);
+        hy = hy + s.tab_at(FDTD_TAB_C2, col) * psi;
+    }
+    s.Hy(k) = hy;
+}
+
+// The TF/SF correction for a cell the H loop does not visit (nzsrc-1 == 0 or >= nz).
+template <typename T, class S>
+__device__ __forceinline__ void tfsf_edge(const FdtdInstance &I, S &s, T src_h)
+{
+    const int j = I.nzsrc - 1;
+    if (I.tfsf && (j <= 0 || j >= I.nz) && j >= 0 && j <= I.nz) s.Hy(j) = s.Hy(j) - src_h;
+}
+
+template <typename T>
+struct BatchArgs {
+    int n_inst;
+    const FdtdInstance *inst;
+    const int32_t *order;
+    const double *pml_tab;
+    const double *src;
+    T *state;
+    T *probe;
+    T *hist;
+    int32_t *queue;
+    int32_t *status;
+    int32_t *fallbacks;
+    int64_t smem_bytes;
+};
+
+template <typename T>
+__host__ __device__ inline int64_t resident_elems(const FdtdInstance &I)
+{
+    const int64_t n = (int64_t)I.nz + 1;
+    const int64_t S = (I.mode == FDTD_MODE_FREESPACE) ? 0 : (int64_t)(I.rear - I.front);
+    const int64_t nslab = (I.mode == FDTD_MODE_LINLOR) ? 3 : (I.mode == FDTD_MODE_KERR ? 1 : 0);
+    const int64_t W = 2 * (int64_t)I.pml + 1;
+    return 2 * n + nslab * (S > 0 ? S : 0) + 2 * W + FDTD_TAB_ROWS * W;
+}
+
+// One instance, all requested steps, fields resident in shared memory.
+template <typename T>
+__device__ void run_instance_resident(const BatchArgs<T> &args, int idx, T *smem)
+{
+    const FdtdInstance I = args.inst[idx];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int n = I.nz + 1;
+    const int W = 2 * I.pml + 1;
+    const int S = (I.mode == FDTD_MODE_FREESPACE) ? 0 : (I.rear - I.front);
+    T *gst = args.state + I.state_offset;
+    T *gEx = gst + (int64_t)FDTD_ST_EX * n, *gHy = gst + (int64_t)FDTD_ST_HY * n;
+    T *gDx = gst + (int64_t)FDTD_ST_DX * n, *gP = gst + (int64_t)FDTD_ST_P * n;
+    T *gPp = gst + (int64_t)FDTD_ST_PPREV * n, *gPsiE = gst + (int64_t)FDTD_ST_PSIE * n;
+    T *gPsiH = gst + (int64_t)FDTD_ST_PSIH * n, *gA = gst + (int64_t)FDTD_ST_A * n;
+
+    SmemStore<T> s;
+    T *q = smem;
+    s.ex = q; q += n;
+    s.hy = q; q += n;
+    s.dx = q; q += (I.mode != FDTD_MODE_FREESPACE) ? S : 0;
+    s.p = q; q += (I.mode == FDTD_MODE_LINLOR) ? S : 0;
+    s.pp = q; q += (I.mode == FDTD_MODE_LINLOR) ? S : 0;
+    s.psie = q; q += W;
+    s.psih = q; q += W;
+    s.tab = q;
+    s.front = I.front;
+    s.W = W;
+
+    const double *tab = args.pml_tab + I.pml_offset;
+    for (int i = tid; i < FDTD_TAB_ROWS * W; i += nt) s.tab[i] = (T)tab[i];
+    // initial state
+    if (I.resume) {
+        for (int k = tid; k < n; k += nt) { s.ex[k] = gEx[k]; s.hy[k] = gHy[k]; }
+        for (int j = tid; j < S; j += nt) {
+            s.dx[j] = gDx[I.front + j];
+            if (I.mode == FDTD_MODE_LINLOR) { s.p[j] = gP[I.front + j]; s.pp[j] = gPp[I.front + j]; }
+        }
+        for (int cidx = tid; cidx < W; cidx += nt) {
+            const int k = (cidx <= I.pml) ? cidx : (n - I.pml + (cidx - I.pml - 1));
+            s.psie[cidx] = gPsiE[k];
+            s.psih[cidx] = gPsiH[k];
+        }
+    } else {
+        for (int k = tid; k < n; k += nt) { s.ex[k] = T(0); s.hy[k] = T(0); }
+        for (int j = tid; j < S; j += nt) {
+            s.dx[j] = T(0);
+            if (I.mode == FDTD_MODE_LINLOR) { s.p[j] = T(0); s.pp[j] = T(0); }
+        }
+        for (int cidx = tid; cidx < W; cidx += nt) { s.psie[cidx] = T(0); s.psih[cidx] = T(0); }
+        if (I.mode == FDTD_MODE_KERR)
+            for (int k = tid; k < n; k += nt) gA[k] = T(0);
+    }
+    __syncthreads();
+
+    const Scal<T> c = make_scal<T>(I);
+    Kerr<T> kr;
+    kr.setup(I);
+    const double *Exs = args.src + I.src_offset;
+    const double *Hys = Exs + I.n_steps;
+    T *probe = args.probe + I.probe_offset;
+    T *hist = args.hist ? args.hist + I.hist_offset : nullptr;
+    int nfb = 0;
+
+    for (int t = I.step_begin; t < I.step_end; ++t) {
+        const T src_e = (T)(Exs[t] / I.sc);
+        const T src_h = I.tfsf ? (T)(Hys[t] / I.sc) : T(0);
+        T *a_out = (t == I.step_end - 1) ? gA : nullptr;
+        for (int k = 1 + tid; k < n; k += nt)
+            e_cell<T>(I, c, kr, s, k, src_e, src_h, (const T *)nullptr, a_out, &nfb);
+        __syncthreads();
+        for (int k = 1 + tid; k < n - 1; k += nt) h_cell<T>(I, c, s, k, src_h);
+        if (tid == 0) tfsf_edge<T>(I, s, src_h);
+        // probes and snapshots read Ex, which the H phase does not write
+        if (tid < 2 && t >= I.probe_lo[tid] && t <= I.probe_hi[tid])
+            probe[(int64_t)t * 2 + tid] = s.ex[I.probe_cell[tid]];
+        if (hist && I.hist_interval > 0 && t > 0 && (t % I.hist_interval) == 0) {
+            const int row = t / I.hist_interval;
+            if (row < I.hist_rows)
+                for (int k = tid; k < n; k += nt) hist[(int64_t)row * n + k] = s.ex[k];
+        }
+        __syncthreads();
+    }
+
+    // write back the full-length state
+    bool bad = false;
+    for (int k = tid; k < n; k += nt) {
+        const T e = s.ex[k], h = s.hy[k];
+        gEx[k] = e;
+        gHy[k] = h;
+        bad |= !(isfinite((double)e) && isfinite((double)h));
+        const bool in_slab = (k >= I.front && k < I.rear);
+        gDx[k] = (I.mode != FDTD_MODE_FREESPACE && in_slab) ? s.dx[k - I.front] : T(0);
+        gP[k] = (I.mode == FDTD_MODE_LINLOR && in_slab) ? s.p[k - I.front] : T(0);
+        gPp[k] = (I.mode == FDTD_MODE_LINLOR && in_slab) ? s.pp[k - I.front] : T(0);
+        const int col = pml_col(I, k);
+        gPsiE[k] = (col >= 0) ? s.psie[col] : T(0);
+        gPsiH[k] = (col >= 0) ? s.psih[col] : T(0);
+        if (I.mode != FDTD_MODE_KERR) gA[k] = T(0);
+    }
+    if (bad && args.status) atomicOr(args.status + idx, FDTD_STATUS_NONFINITE);
+    if (nfb && args.fallbacks) atomicAdd(args.fallbacks + idx, nfb);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) fdtd_batch_kernel(BatchArgs<T> args)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int next;
+    T *smem = reinterpret_cast<T *>(smem_raw);
+    while (true) {
+        if (threadIdx.x == 0) next = atomicAdd(args.queue, 1);
+        __syncthreads();
+        const int q = next;
+        __syncthreads();
+        if (q >= args.n_inst) break;
+        const int idx = args.order ? args.order[q] : q;
+        if (resident_elems<T>(args.inst[idx]) * (int64_t)sizeof(T) > args.smem_bytes) {
+            if (threadIdx.x == 0 && args.status) atomicOr(args.status + idx, FDTD_STATUS_SKIPPED);
+            continue;
+        }
+        run_instance_resident<T>(args, idx, smem);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// global-memory path: one instance of any size, two launches per step
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__device__ inline GlobalStore<T> global_store(const FdtdInstance &I, const BatchArgs<T> &args)
+{
+    const int n = I.nz + 1;
+    T *gst = args.state + I.state_offset;
+    GlobalStore<T> s;
+    s.ex = gst + (int64_t)FDTD_ST_EX * n;
+    s.hy = gst + (int64_t)FDTD_ST_HY * n;
+    s.dx = gst + (int64_t)FDTD_ST_DX * n;
+    s.p = gst + (int64_t)FDTD_ST_P * n;
+    s.pp = gst + (int64_t)FDTD_ST_PPREV * n;
+    s.psie = gst + (int64_t)FDTD_ST_PSIE * n;
+    s.psih = gst + (int64_t)FDTD_ST_PSIH * n;
+    s.tab = args.pml_tab + I.pml_offset;
+    s.W = 2 * I.pml + 1;
+    return s;
+}
+
+template <typename T>
+__global__ void fdtd_global_e_kernel(BatchArgs<T> args, int t)
+{
+    const FdtdInstance &I = args.inst[0];
+    GlobalStore<T> s = global_store<T>(I, args);
+    const Scal<T> c = make_scal<T>(I);
+    Kerr<T> kr;
+    kr.setup(I);
+    const double *Exs = args.src + I.src_offset;
+    const double *Hys = Exs + I.n_steps;
+    const T src_e = (T)(Exs[t] / I.sc);
+    const T src_h = I.tfsf ? (T)(Hys[t] / I.sc) : T(0);
+    const int n = I.nz + 1;
+    T *gA = args.state + I.state_offset + (int64_t)FDTD_ST_A * n;
+    int nfb = 0;
+    for (int k = 1 + blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        e_cell<T>(I, c, kr, s, k, src_e, src_h, (const T *)nullptr, gA, &nfb);
+    if (nfb && args.fallbacks) atomicAdd(args.fallbacks, nfb);
+}
+
+template <typename T>
+__global__ void fdtd_global_h_kernel(BatchArgs<T> args, int t)
+{
+    const FdtdInstance &I = args.inst[0];
+    GlobalStore<T> s = global_store<T>(I, args);
+    const Scal<T> c = make_scal<T>(I);
+    const double *Hys = args.src + I.src_offset + I.n_steps;
+    const T src_h = I.tfsf ? (T)(Hys[t] / I.sc) : T(0);
+    const int n = I.nz + 1;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int k = 1 + gt; k < n - 1; k += gridDim.x * blockDim.x) h_cell<T>(I, c, s, k, src_h);
+    if (gt == 0) tfsf_edge<T>(I, s, src_h);
+}
+
+// Probes and snapshots after the H phase (they read Ex only).
+template <typename T>
+__global__ void fdtd_global_probe_kernel(BatchArgs<T> args, int t)
+{
+    const FdtdInstance &I = args.inst[0];
+    const int n = I.nz + 1;
+    const T *ex = args.state + I.state_offset + (int64_t)FDTD_ST_EX * n;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gt < 2 && t >= I.probe_lo[gt] && t <= I.probe_hi[gt])
+        args.probe[I.probe_offset + (int64_t)t * 2 + gt] = ex[I.probe_cell[gt]];
+    if (args.hist && I.hist_interval > 0 && t > 0 && (t % I.hist_interval) == 0) {
+        const int row = t / I.hist_interval;
+        if (row < I.hist_rows)
+            for (int k = gt; k < n; k += gridDim.x * blockDim.x)
+                args.hist[I.hist_offset + (int64_t)row * n + k] = ex[k];
+    }
+}
+
+template <typename T>
+__global__ void fdtd_global_init_kernel(BatchArgs<T> args)
+{
+    const FdtdInstance &I = args.inst[0];
+    const int64_t n = (int64_t)I.nz + 1;
+    T *gst = args.state + I.state_offset;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < FDTD_STATE_ARRAYS * n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        gst[i] = T(0);
+}
+
+template <typename T>
+__global__ void fdtd_global_finish_kernel(BatchArgs<T> args)
+{
+    const FdtdInstance &I = args.inst[0];
+    const int n = I.nz + 1;
+    const T *gst = args.state + I.state_offset;
+    bool bad = false;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        bad |= !(isfinite((double)gst[k]) && isfinite((double)gst[n + k]));
+    if (bad && args.status) atomicOr(args.status, FDTD_STATUS_NONFINITE);
+}
+
+}  // namespace fdtdpic
