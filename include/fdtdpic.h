@@ -157,6 +157,61 @@ int fdtd1d_run_global(int precision, const FdtdInstance *h_inst, const FdtdInsta
  * d_coef: n x 4 doubles (a,b,c,d); d_out: n doubles. */
 int fdtdpic_cubic_root0(int n, const double *d_coef, double *d_out, fdtdpic_stream_t stream);
 
+/* ---- FDTD + electron-beam PIC -------------------------------------------------------------
+ * Replaces the reference's Jx hook (MasterController.py:93,159; the -Jx term of ADE_ExUpdate,
+ * BaseFDTD11.py:667), which the reference never fills; the beam model has no reference code.
+ * Particles: position = cell (int32) + frac in [0,1) in units of dz; momentum u/c = gamma v/c
+ * (ux, uz).  Each step: gather E^t and B^t = -mu0 (Hy + Hyp)/2 by CIC, relativistic Boris push,
+ * Jx deposited by CIC at the half-step midpoint, Jz charge-conserving on half nodes, periodic
+ * wrap into [clo, chi); then the field step of the instance's mode with -Jx in the Ex (and slab
+ * Dx) update.  Deposits are exact int64 fixed-point sums (scale jscale), so results do not depend
+ * on particle order or thread scheduling; particles are re-binned by cell every sort_every
+ * steps so each CTA's deposits stay in a small shared-memory window. */
+typedef struct PicBeam {
+    int32_t n_part;     /* macroparticles */
+    int32_t clo, chi;   /* periodic beam domain, cells [clo, chi); 2 <= clo < chi <= nz-2 */
+    int32_t sort_every; /* re-bin by cell every this many steps (0: never) */
+    int32_t chunk;      /* particles per CTA in the push kernel (0: library default) */
+    int32_t reserved;
+    double kE;     /* q dt / (2 m c) */
+    double kH;     /* -q mu0 dt / (2 m) */
+    double sc;     /* c dt / dz */
+    double kJ;     /* q w c: Jx per unit ux/gamma */
+    double kJz;    /* q w dz / dt: Jz per unit cell displacement */
+    double jscale; /* deposit fixed-point scale, a power of two; see fdtdpic_pic_jscale */
+} PicBeam;
+
+/* Optional per-kernel GPU time of one fdtdpic_run call, from CUDA events recorded around every
+ * launch (milliseconds summed over the call).  Passing a timing struct makes the call
+ * synchronous and launches kernel by kernel instead of replaying captured graphs. */
+typedef struct FdtdPicTiming {
+    float push_ms;  /* gather + Boris push + deposit */
+    float field_ms; /* field step (E and H phases) */
+    float sort_ms;  /* re-binning by cell */
+    int32_t steps;
+} FdtdPicTiming;
+
+/* Bytes of caller scratch fdtdpic_run needs (deposit accumulators, re-binning buffers). */
+int64_t fdtdpic_scratch_bytes(int precision, int nz, int n_part);
+/* The largest power-of-two scale for which no deposit accumulator can overflow. */
+double fdtdpic_pic_jscale(const PicBeam *beam);
+
+/* Steps [step_begin, step_end) of one instance coupled to a beam.  Fields live in d_state (as
+ * fdtd1d_run_global); d_hyp (nz+1) holds Hy one half step back (zero for a fresh run) and is
+ * updated.  Particle arrays (n_part each, T = precision's type): d_cell int32, d_frac, d_ux,
+ * d_uz T, d_id int32 (an identity carried through re-binning); updated in place (re-binning
+ * permutes them within each cell).  d_jx/d_jz (nz+1, T) receive the last step's grid currents.
+ * d_status[0] += particles that left the grid, d_status[1] |= FDTD_STATUS_NONFINITE.
+ * Blocks of 2*sort_every steps (64 without re-binning) are captured once into a CUDA graph and
+ * replayed (the step index lives in the scratch), so a repeated call with the same arguments
+ * reuses the graph; timing (nullable) is described at FdtdPicTiming. */
+int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d_inst,
+                const double *d_pml_tab, const double *d_src, void *d_state, void *d_probe,
+                const PicBeam *beam, int32_t *d_cell, void *d_frac, void *d_ux, void *d_uz,
+                int32_t *d_id, void *d_jx, void *d_jz, void *d_hyp, void *d_scratch,
+                int64_t scratch_bytes, int32_t *d_status, FdtdPicTiming *timing,
+                fdtdpic_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -115,8 +115,8 @@ double or_cubic_root0(double a, double b, double c, double d)
  *   hist         every hist_interval steps (k>0, k%hist_interval==0, k/hist_interval<hist_rows)
  *                Ex is copied to hist_out[(k/hist_interval)*(nz+1)]
  */
-int or_run_pass(int mode, int pol_active, int nz, int n_steps, int pml, int cpml_lo, int cpml_hi,
-                int front, int rear, int nzsrc, int tfsf,
+int or_run_pass(int mode, int pol_active, int nz, int t0, int n_steps, int pml, int cpml_lo,
+                int cpml_hi, int front, int rear, int nzsrc, int tfsf, int dx_jx,
                 const double *const *coef, const double *scal, const double *scal2,
                 const double *Exs, const double *Hys, double sc,
                 double *Ex, double *Hy, double *Dx, double *P, double *Pprev, double *psiE,
@@ -134,7 +134,7 @@ int or_run_pass(int mode, int pol_active, int nz, int n_steps, int pml, int cpml
     const int len = nz + 1;
     const int cpml = cpml_lo || cpml_hi;
 
-    for (int t = 0; t < n_steps; ++t) {
+    for (int t = t0; t < t0 + n_steps; ++t) {
         if (mode == OR_LINLOR && pol_active) {
             for (int k = front; k < rear; ++k) {
                 double pm2 = Pprev[k];      /* tempTempVarPol after ADE_TempPolCurr */
@@ -159,8 +159,12 @@ int or_run_pass(int mode, int pol_active, int nz, int n_steps, int pml, int cpml
         Ex[nzsrc] += Exs[t] / sc;
         if (tfsf) Hy[nzsrc - 1] -= Hys[t] / sc;
         if (mode == OR_LINLOR || mode == OR_KERR) {
-            for (int k = front; k < rear; ++k)
-                Dx[k] = Dx[k] + (Hy[k] - Hy[k - 1]) * (dtdz) * denE[k];
+            if (dx_jx)
+                for (int k = front; k < rear; ++k)
+                    Dx[k] = Dx[k] + (Hy[k] - Hy[k - 1] - Jx[k]) * (dtdz) * denE[k];
+            else
+                for (int k = front; k < rear; ++k)
+                    Dx[k] = Dx[k] + (Hy[k] - Hy[k - 1]) * (dtdz) * denE[k];
         }
         if (mode == OR_KERR) {
             for (int k = front; k < rear; ++k) {

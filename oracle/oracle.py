@@ -82,8 +82,10 @@ def lib():
         _lib.or_cubic_solve.restype = None
         _lib.or_cubic_solve.argtypes = [d, d, d, d, P, P, P]
         _lib.or_run_pass.restype = i
-        _lib.or_run_pass.argtypes = ([i] * 11 + [P, P, P, P, P, d] + [P] * 9 + [i, P, i, i, P]
+        _lib.or_run_pass.argtypes = ([i] * 13 + [P, P, P, P, P, d] + [P] * 9 + [i, P, i, i, P]
                                      + [i, i, P])
+        _lib.or_pic_step.restype = i
+        _lib.or_pic_step.argtypes = [i, P, P, P, P, P, P, P, P, P, i, P, i]
     return _lib
 
 
@@ -471,8 +473,8 @@ def _run(mode, pol_active, P: RefParams, coef, scal, scal2, Exs, Hys, st, probe_
     pc = np.ascontiguousarray(probe_cells, dtype=np.int32)
     hist_rows = 0 if hist is None else hist.shape[0]
     rc = lib().or_run_pass(
-        mode, pol_active, P.Nz, P.timeSteps, P.pmlWidth, int(P.CPMLXm), int(P.CPMLXp),
-        P.materialFrontEdge, P.materialRearEdge, P.nzsrc, int(P.TFSF),
+        mode, pol_active, P.Nz, 0, P.timeSteps, P.pmlWidth, int(P.CPMLXm), int(P.CPMLXp),
+        P.materialFrontEdge, P.materialRearEdge, P.nzsrc, int(P.TFSF), 0,
         ptrs, _p(sc), _p(sc2), _p(Exs), _p(Hys), P.courantNo,
         _p(st["Ex"]), _p(st["Hy"]), _p(st["Dx"]), _p(st["P"]), _p(st["Pprev"]), _p(st["psiE"]),
         _p(st["psiH"]), _p(st["A"]), _p(st["Jx"]),
@@ -680,3 +682,89 @@ def rel_l2(a, b):
 
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv))
+
+
+# -------------------------------------------------------------------------------------------
+# electron-beam PIC (no reference counterpart; model stated in pic_oracle.c)
+# -------------------------------------------------------------------------------------------
+Q_E = -1.602176634e-19  # electron charge [C]
+M_E = 9.1093837139e-31  # electron mass [kg]
+
+
+def pic_constants(dz, dt, weight, mu0, q=Q_E, m=M_E):
+    """(kE, kH, sc, kJ, kJz) of the Boris step in normalised momentum u/c."""
+    return dict(kE=q * dt / (2.0 * m * C0), kH=-q * mu0 * dt / (2.0 * m), sc=C0 * dt / dz,
+                kJ=q * weight * C0, kJz=q * weight * dz / dt)
+
+
+def beam(n_part, clo, chi, v_mean=0.3, v_spread=0.003, seed=20261203):
+    """Seeded beam: zeta ~ U[clo, chi) (cells), vz ~ N(v_mean c, v_spread c), vx = 0.
+    Returned sorted by position as (cell int32, frac, ux, uz) with u = gamma v / c."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    zeta = clo + (chi - clo) * rng.random(n_part)
+    vz = rng.normal(v_mean, v_spread, n_part)
+    uz = vz / np.sqrt(1.0 - vz * vz)
+    order = np.argsort(zeta, kind="stable")
+    zeta, uz = zeta[order], uz[order]
+    cell = np.floor(zeta).astype(np.int32)
+    return cell, zeta - cell, np.zeros(n_part), uz.copy()
+
+
+def _pass_setup(P: RefParams, mode, pf):
+    if mode == FREESPACE:
+        upHy, upEx = material_update_coef(P)
+    else:
+        upHy, upEx = empty_space(P)
+    coef = cpml_coefficients(P, upEx)
+    coef.update(upEx=upEx, upHy=upHy)
+    cub, qua, one, e0r, e0chi = _kerr_scalars(P, pf)
+    A, B, C = _lorentz_scalars(P, pf)
+    scal = [P.delT / (P.dz), P.permit_0, A, B, C, cub, qua, one]
+    return coef, scal, [e0r, e0chi]
+
+
+def integrate_pic(P: RefParams, mode, Exs, Hys, cell, frac, ux, uz, consts, clo, chi, n_steps=None,
+                  probe_cells=(50, 950), n_threads=1, apply_stab=True):
+    """One FDTD pass (Kerr, Lorentz with polarisation on, or free space) coupled to the beam:
+    each step pushes/deposits, then runs the field step with Jx.  Particle arrays are updated
+    in place.  Returns a dict of fields, last-step Jx/Jz and probe traces."""
+    T = P.timeSteps if n_steps is None else n_steps
+    n = P.Nz + 1
+    pf = P.plasmaFreqE
+    if apply_stab and mode != FREESPACE:
+        pf = spatial_stab(P.timeSteps, P.Nz, P.dz, P.freq_in, P.delT, pf, P.omega_0E,
+                          P.gammaE)[3]
+    coef, scal, scal2 = _pass_setup(P, mode, pf)
+    st = _fresh_state(n)
+    Hyp = np.zeros(n)
+    Jz = np.zeros(n)
+    cells = np.ascontiguousarray(probe_cells, np.int32)
+    pr = np.zeros((P.timeSteps, len(cells)))
+    pscal = np.array([clo, chi, consts["kE"], consts["kH"], consts["sc"], consts["kJ"],
+                      consts["kJz"]], np.float64)
+    arrs = [np.ascontiguousarray(coef[k], dtype=np.float64) for k in
+            ("upEx", "upHy", "den_Exdz", "den_Hydz", "beX", "ceX", "Cb", "bmY", "cmY", "C2")]
+    ptrs = (ctypes.c_void_p * 10)(*[a.ctypes.data for a in arrs])
+    sc_ = np.ascontiguousarray(scal, np.float64)
+    sc2 = np.ascontiguousarray(scal2, np.float64)
+    Exs = np.ascontiguousarray(Exs, np.float64)
+    Hys = np.ascontiguousarray(Hys if len(Hys) else np.zeros(P.timeSteps), np.float64)
+    L = lib()
+    lost = 0
+    for t in range(T):
+        hy_now = st["Hy"].copy()
+        lost += L.or_pic_step(len(cell), _p(cell), _p(frac), _p(ux), _p(uz), _p(st["Ex"]), _p(st["Hy"]),
+                              _p(Hyp), _p(st["Jx"]), _p(Jz), P.Nz, _p(pscal), n_threads)
+        rc = L.or_run_pass(mode, 1, P.Nz, t, 1, P.pmlWidth, int(P.CPMLXm), int(P.CPMLXp),
+                           P.materialFrontEdge, P.materialRearEdge, P.nzsrc, int(P.TFSF), 1,
+                           ptrs, _p(sc_), _p(sc2), _p(Exs), _p(Hys), P.courantNo,
+                           _p(st["Ex"]), _p(st["Hy"]), _p(st["Dx"]), _p(st["P"]),
+                           _p(st["Pprev"]), _p(st["psiE"]), _p(st["psiH"]), _p(st["A"]),
+                           _p(st["Jx"]), len(cells), _p(cells), 0, P.timeSteps - 1, _p(pr),
+                           0, 0, None)
+        if rc != 0:
+            raise ValueError("oracle stepping rejected its arguments")
+        Hyp = hy_now
+    return dict(Ex=st["Ex"], Hy=st["Hy"], Dx=st["Dx"], P=st["P"], Acubic=st["A"],
+                psi_Ex=st["psiE"], psi_Hy=st["psiH"], Jx=st["Jx"], Jz=Jz, Hyp=Hyp,
+                probes=pr[:T], lost=lost, plasmaFreqE=float(pf))

@@ -1,7 +1,11 @@
 // C ABI of libfdtdpic.so: argument checks and dispatch to the typed launchers.
 #include <stddef.h>
+#include <string.h>
+
+#include <math.h>
 
 #include "fdtd1d_launch.cuh"
+#include "pic_kernel.cuh"
 
 namespace fdtdpic {
 
@@ -20,6 +24,50 @@ int run_batch_f32(const BatchArgs<float> &a, int threads, int grid, cudaStream_t
 int run_global_f64(const FdtdInstance &h, const BatchArgs<double> &a, cudaStream_t st);
 int run_global_f32(const FdtdInstance &h, const BatchArgs<float> &a, cudaStream_t st);
 int run_cubic_root0(int n, const double *coef, double *out, cudaStream_t st);
+int run_pic_f64(const FdtdInstance &h, const BatchArgs<double> &fa, const PicBeam &bm,
+                int32_t *cell, double *frac, double *ux, double *uz, int32_t *id, double *jx,
+                double *jz, double *hyp, unsigned char *scratch, int32_t *status,
+                FdtdPicTiming *timing, cudaStream_t st);
+int run_pic_f32(const FdtdInstance &h, const BatchArgs<float> &fa, const PicBeam &bm,
+                int32_t *cell, float *frac, float *ux, float *uz, int32_t *id, float *jx,
+                float *jz, float *hyp, unsigned char *scratch, int32_t *status,
+                FdtdPicTiming *timing, cudaStream_t st);
+
+// ---- captured PIC step blocks (replayed by calls with identical arguments) -------------
+static PicGraphEntry g_graphs[16];
+static int g_graph_count = 0, g_graph_next = 0;
+
+PicGraphEntry *pic_graph_lookup(const void *key, size_t len)
+{
+    for (int i = 0; i < g_graph_count; ++i)
+        if (g_graphs[i].key_len == len && memcmp(g_graphs[i].key, key, len) == 0) return &g_graphs[i];
+    return nullptr;
+}
+
+void pic_graph_store(const void *key, size_t len, cudaGraphExec_t exec)
+{
+    if (len > sizeof(g_graphs[0].key)) return;
+    PicGraphEntry &e = g_graphs[g_graph_next];
+    if (g_graph_next < g_graph_count && e.exec) {
+        cudaDeviceSynchronize();  // the evicted graph may still be running
+        cudaGraphExecDestroy(e.exec);
+    }
+    memcpy(e.key, key, len);
+    e.key_len = len;
+    e.exec = exec;
+    g_graph_next = (g_graph_next + 1) % 16;
+    if (g_graph_count < 16) ++g_graph_count;
+}
+
+cudaStream_t pic_capture_stream()
+{
+    static cudaStream_t streams[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    if (!streams[dev] && cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking) != cudaSuccess)
+        return nullptr;
+    return streams[dev];
+}
 
 static int check_instance(const FdtdInstance &I)
 {
@@ -159,6 +207,57 @@ int fdtdpic_cubic_root0(int n, const double *d_coef, double *d_out, fdtdpic_stre
 {
     if (n < 0 || (n > 0 && (!d_coef || !d_out))) return FDTDPIC_ERR_ARG;
     return run_cubic_root0(n, d_coef, d_out, (cudaStream_t)stream);
+}
+
+int64_t fdtdpic_scratch_bytes(int precision, int nz, int n_part)
+{
+    if ((precision != FDTDPIC_F64 && precision != FDTDPIC_F32) || nz < 2 || n_part < 0) return 0;
+    return (int64_t)pic_scratch_layout(precision, nz, n_part).total;
+}
+
+double fdtdpic_pic_jscale(const PicBeam *bm)
+{
+    if (!bm || bm->n_part < 0) return 0.0;
+    // |one node's sum| <= n_part * max(|kJ|, |kJz|) (|ux/gamma| < 1, |cell displacement| < 1)
+    const double bound = (double)(bm->n_part > 0 ? bm->n_part : 1) *
+                         fmax(fabs(bm->kJ), fabs(bm->kJz)) * 1.0001;
+    if (!(bound > 0.0) || !isfinite(bound)) return 1.0;
+    const int S = (int)floor(62.0 - log2(bound));
+    return ldexp(1.0, S);
+}
+
+int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d_inst,
+                const double *d_pml_tab, const double *d_src, void *d_state, void *d_probe,
+                const PicBeam *beam, int32_t *d_cell, void *d_frac, void *d_ux, void *d_uz,
+                int32_t *d_id, void *d_jx, void *d_jz, void *d_hyp, void *d_scratch,
+                int64_t scratch_bytes, int32_t *d_status, FdtdPicTiming *timing,
+                fdtdpic_stream_t stream)
+{
+    if (!h_inst || !d_inst || !d_pml_tab || !d_src || !d_state || !d_probe || !beam || !d_jx ||
+        !d_jz || !d_hyp || !d_scratch || !d_status)
+        return FDTDPIC_ERR_ARG;
+    int rc = check_instance(*h_inst);
+    if (rc != FDTDPIC_OK) return rc;
+    const PicBeam &b = *beam;
+    if (b.n_part < 0 || b.clo < 2 || b.chi <= b.clo || b.chi > h_inst->nz - 2 || b.sort_every < 0 ||
+        b.chunk < 0 || !(b.jscale > 0.0))
+        return FDTDPIC_ERR_ARG;
+    if (b.n_part > 0 && (!d_cell || !d_frac || !d_ux || !d_uz || !d_id)) return FDTDPIC_ERR_ARG;
+    if (precision != FDTDPIC_F64 && precision != FDTDPIC_F32) return FDTDPIC_ERR_ARG;
+    if (scratch_bytes < fdtdpic_scratch_bytes(precision, h_inst->nz, b.n_part)) return FDTDPIC_ERR_OOM;
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned char *scr = (unsigned char *)d_scratch;
+    if (precision == FDTDPIC_F64) {
+        BatchArgs<double> a{1, d_inst, nullptr, d_pml_tab, d_src, (double *)d_state,
+                            (double *)d_probe, nullptr, nullptr, nullptr, nullptr, 0};
+        return run_pic_f64(*h_inst, a, b, d_cell, (double *)d_frac, (double *)d_ux,
+                           (double *)d_uz, d_id, (double *)d_jx, (double *)d_jz,
+                           (double *)d_hyp, scr, d_status, timing, st);
+    }
+    BatchArgs<float> a{1, d_inst, nullptr, d_pml_tab, d_src, (float *)d_state, (float *)d_probe,
+                       nullptr, nullptr, nullptr, nullptr, 0};
+    return run_pic_f32(*h_inst, a, b, d_cell, (float *)d_frac, (float *)d_ux, (float *)d_uz,
+                       d_id, (float *)d_jx, (float *)d_jz, (float *)d_hyp, scr, d_status, timing, st);
 }
 
 }  // extern "C"

@@ -109,10 +109,12 @@ struct GlobalStore {
 };
 
 // E phase for cell k in [1, nz].  src_e = Exs[t]/Sc, src_h = Hys[t]/Sc in T.
+// jx (nullable): the beam's grid current, entering the Ex update as the reference's -Jx term
+// and, with the beam on, the slab's Dx update too (dx_jx).
 template <typename T, class S>
 __device__ __forceinline__ void e_cell(const FdtdInstance &I, const Scal<T> &c, const Kerr<T> &kr,
                                        S &s, int k, T src_e, T src_h, const T *jx, T *a_out,
-                                       int *nfb)
+                                       int *nfb, bool dx_jx = false)
 {
     const int n = I.nz + 1;
     const T hk = s.Hy(k), hkm = s.Hy(k - 1);
@@ -142,7 +144,9 @@ __device__ __forceinline__ void e_cell(const FdtdInstance &I, const Scal<T> &c, 
             if (k == I.nzsrc - 1) hk_d = hk - src_h;
             if (k == I.nzsrc) hkm_d = hkm - src_h;
         }
-        const T dx = s.Dx(k) + (hk_d - hkm_d) * c.dtdz * den;
+        T dhd = hk_d - hkm_d;
+        if (dx_jx && jx) dhd = dhd - jx[k];
+        const T dx = s.Dx(k) + dhd * c.dtdz * den;
         s.Dx(k) = dx;
         if (I.mode == FDTD_MODE_KERR) {
             const T A = kr.root(dx, c.eps0, nfb);

@@ -1,0 +1,620 @@
+// Electron-beam PIC coupled to the 1D FDTD grid, templated on the state type T.
+//
+// Per step t (fields: E^t, H^(t+1/2) in Hy, H^(t-1/2) in Hyp):
+//   pic_push_kernel : gather, relativistic Boris push, move, deposit Jx^(t+1/2) and Jz into
+//                     int64 fixed-point accumulators (exact integer sums: bit-identical results
+//                     for any particle order or thread schedule; no float atomics)
+//   pic_e_kernel    : Hyp <- Hy; Jx, Jz <- accumulators (then zeroed); E phase with -Jx
+//   pic_h_kernel    : H phase, probes, snapshots
+// and every sort_every steps a counting re-bin of the particles by cell (histogram, scan,
+// scatter), which keeps each CTA's particles within a few cells so its deposits land in a small
+// shared-memory window and warp lanes share nodes (warp-segmented sums via __match_any_sync).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fdtd1d_kernel.cuh"
+
+namespace fdtdpic {
+
+int cuda_status(cudaError_t e);
+
+constexpr int PIC_WIN = 256;      // shared-memory deposit window (nodes) per CTA
+constexpr int PIC_THREADS = 256;  // push kernel CTA size
+
+// Fixed-point words per current component: FP32 keeps one int64 word (scale 2^S),
+// FP64 two (the remainder below 2^-S kept at a further 2^40).
+template <typename T>
+struct Fix;
+template <>
+struct Fix<float> {
+    static constexpr int W = 1;
+    __device__ static void split(float v, double scale, float scale_f, long long *w)
+    {
+        w[0] = __float2ll_rn(v * scale_f);
+    }
+    __device__ static float join(const unsigned long long *w, double inv, float inv_f)
+    {
+        return __ll2float_rn((long long)w[0]) * inv_f;
+    }
+};
+template <>
+struct Fix<double> {
+    static constexpr int W = 2;
+    __device__ static void split(double v, double scale, float, long long *w)
+    {
+        const double x = v * scale;
+        const double hi = floor(x);
+        w[0] = (long long)hi;
+        w[1] = __double2ll_rn((x - hi) * 1099511627776.0);  // 2^40
+    }
+    __device__ static double join(const unsigned long long *w, double inv, float)
+    {
+        return (double)(long long)w[0] * inv + (double)(long long)w[1] * (inv * (1.0 / 1099511627776.0));
+    }
+};
+
+template <typename T>
+struct PicArgs {
+    int n_part, nz, clo, chi, chunk;
+    T kE, kH, sc, kJ, kJz;
+    double jscale, jinv;
+    float jscale_f, jinv_f;
+    int32_t *cell;
+    T *frac, *ux, *uz;
+    const T *ex, *hy, *hyp;
+    unsigned long long *acc;  // [2*W][nz+1]: Jx words then Jz words
+    int32_t *status;
+};
+
+// Sum a uint64 over the lanes of `peers` exactly (wrap-around two's complement arithmetic).
+__device__ __forceinline__ unsigned long long peer_sum_u64(unsigned peers, unsigned long long v)
+{
+    const unsigned c0 = (unsigned)(v & 0x3FFFFFull);
+    const unsigned c1 = (unsigned)((v >> 22) & 0x3FFFFFull);
+    const unsigned c2 = (unsigned)(v >> 44);
+    const unsigned long long s0 = __reduce_add_sync(peers, c0);
+    const unsigned long long s1 = __reduce_add_sync(peers, c1);
+    const unsigned long long s2 = __reduce_add_sync(peers, c2);
+    return s0 + (s1 << 22) + (s2 << 44);
+}
+
+// One deposit slot for the whole warp (every lane calls it; invalid lanes pass node = -1).
+template <int W>
+__device__ __forceinline__ void deposit_slot(unsigned long long *win, unsigned long long *acc,
+                                             int nz1, int base, int word0, int node,
+                                             const long long *val)
+{
+    const unsigned peers = __match_any_sync(0xffffffffu, node);
+    const int lane = threadIdx.x & 31;
+    const bool leader = (lane == __ffs(peers) - 1);
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        const unsigned long long s = peer_sum_u64(peers, (unsigned long long)val[w]);
+        if (leader && node >= 0 && s != 0ull) {
+            const int rel = node - base;
+            if (rel >= 0 && rel < PIC_WIN)
+                atomicAdd(win + (size_t)(word0 + w) * PIC_WIN + rel, s);
+            else
+                atomicAdd(acc + (size_t)(word0 + w) * nz1 + node, s);
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
+{
+    constexpr int W = Fix<T>::W;
+    __shared__ unsigned long long win[2 * W * PIC_WIN];
+    __shared__ int base_s;
+    const int b0 = blockIdx.x * a.chunk;
+    const int b1 = min(a.n_part, b0 + a.chunk);
+    if (b0 >= b1) return;
+    const int nz1 = a.nz + 1;
+    for (int i = threadIdx.x; i < 2 * W * PIC_WIN; i += blockDim.x) win[i] = 0ull;
+    if (threadIdx.x == 0) base_s = a.cell[b0] - 8;
+    __syncthreads();
+    const int base = base_s;
+    const int Lc = a.chi - a.clo;
+    const int iters = (b1 - b0 + blockDim.x - 1) / blockDim.x;
+    int lost = 0;
+    for (int it = 0; it < iters; ++it) {
+        const int p = b0 + it * blockDim.x + threadIdx.x;
+        bool valid = p < b1;
+        int c = 0;
+        T f = T(0);
+        if (valid) {
+            c = a.cell[p];
+            f = a.frac[p];
+            if (c < 1 || c + 2 > a.nz) { valid = false; ++lost; }
+        }
+        int nx0 = -1, nx1 = -1, nzA = -1, nzB = -1;
+        long long vx0[W], vx1[W], vzA[W], vzB[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) vx0[w] = vx1[w] = vzA[w] = vzB[w] = 0;
+        if (valid) {
+            int j;
+            T fh;
+            if (f >= T(0.5)) { j = c; fh = f - T(0.5); } else { j = c - 1; fh = f + T(0.5); }
+            const T E = (T(1) - f) * a.ex[c] + f * a.ex[c + 1];
+            const T H = (T(1) - fh) * (T(0.5) * (a.hy[j] + a.hyp[j])) +
+                        fh * (T(0.5) * (a.hy[j + 1] + a.hyp[j + 1]));
+            const T uxm = a.ux[p] + a.kE * E;
+            const T uzm = a.uz[p];
+            const T gm = sqrt(T(1) + uxm * uxm + uzm * uzm);
+            const T ty = a.kH * H / gm;
+            const T sy = T(2) * ty / (T(1) + ty * ty);
+            const T uxp = uxm - uzm * ty;
+            const T uzp = uzm + uxm * ty;
+            const T uxn = (uxm - uzp * sy) + a.kE * E;
+            const T uzn = uzm + uxp * sy;
+            const T g = sqrt(T(1) + uxn * uxn + uzn * uzn);
+            const T dz = a.sc * uzn / g;
+            T fm = f + T(0.5) * dz;
+            int cm = c;
+            if (fm >= T(1)) { cm += 1; fm -= T(1); } else if (fm < T(0)) { cm -= 1; fm += T(1); }
+            const T jxv = a.kJ * uxn / g;
+            nx0 = cm;
+            nx1 = cm + 1;
+            Fix<T>::split(jxv * (T(1) - fm), a.jscale, a.jscale_f, vx0);
+            Fix<T>::split(jxv * fm, a.jscale, a.jscale_f, vx1);
+            T f1 = f + dz;
+            int c1 = c;
+            if (f1 >= T(1)) { c1 += 1; f1 -= T(1); } else if (f1 < T(0)) { c1 -= 1; f1 += T(1); }
+            if (c1 == c) {
+                nzA = c;
+                Fix<T>::split(a.kJz * (f1 - f), a.jscale, a.jscale_f, vzA);
+            } else if (c1 == c + 1) {
+                nzA = c;
+                nzB = c + 1;
+                Fix<T>::split(a.kJz * (T(1) - f), a.jscale, a.jscale_f, vzA);
+                Fix<T>::split(a.kJz * f1, a.jscale, a.jscale_f, vzB);
+            } else {
+                nzA = c - 1;
+                nzB = c;
+                Fix<T>::split(-a.kJz * (T(1) - f1), a.jscale, a.jscale_f, vzA);
+                Fix<T>::split(-a.kJz * f, a.jscale, a.jscale_f, vzB);
+            }
+            if (c1 >= a.chi) c1 -= Lc;
+            else if (c1 < a.clo) c1 += Lc;
+            a.cell[p] = c1;
+            a.frac[p] = f1;
+            a.ux[p] = uxn;
+            a.uz[p] = uzn;
+        }
+        deposit_slot<W>(win, a.acc, nz1, base, 0, nx0, vx0);
+        deposit_slot<W>(win, a.acc, nz1, base, 0, nx1, vx1);
+        deposit_slot<W>(win, a.acc, nz1, base, W, nzA, vzA);
+        deposit_slot<W>(win, a.acc, nz1, base, W, nzB, vzB);
+    }
+    if (lost) atomicAdd(a.status, lost);
+    __syncthreads();
+    for (int i = threadIdx.x; i < 2 * W * PIC_WIN; i += blockDim.x) {
+        const unsigned long long v = win[i];
+        const int word = i / PIC_WIN;
+        const int node = base + (i % PIC_WIN);
+        if (v != 0ull && node >= 0 && node < nz1) atomicAdd(a.acc + (size_t)word * nz1 + node, v);
+    }
+}
+
+template <typename T>
+struct PicField {
+    BatchArgs<T> f;
+    unsigned long long *acc;
+    T *jx, *jz, *hyp;
+    double jinv;
+    float jinv_f;
+    const int32_t *step;  // device step counter (graph replay); NULL: use the launch argument
+};
+
+template <typename T>
+__device__ __forceinline__ int pic_step_index(const PicField<T> &a, int t)
+{
+    return a.step ? *a.step : t;
+}
+
+// E phase of cell k with the beam: Hyp <- Hy (H^(t+1/2) for the next push), currents out of the
+// accumulators (which are zeroed for the next push), then the reference E phase with -Jx.
+template <typename T>
+__device__ __forceinline__ void pic_e_cell(PicField<T> &a, const FdtdInstance &I,
+                                           GlobalStore<T> &s, const Scal<T> &c, const Kerr<T> &kr,
+                                           int k, int n, T src_e, T src_h, T *gA, int *nfb)
+{
+    constexpr int W = Fix<T>::W;
+    a.hyp[k] = s.Hy(k);
+    unsigned long long wx[W], wz[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        wx[w] = a.acc[(size_t)w * n + k];
+        wz[w] = a.acc[(size_t)(W + w) * n + k];
+        a.acc[(size_t)w * n + k] = 0ull;
+        a.acc[(size_t)(W + w) * n + k] = 0ull;
+    }
+    a.jx[k] = Fix<T>::join(wx, a.jinv, a.jinv_f);
+    a.jz[k] = Fix<T>::join(wz, a.jinv, a.jinv_f);
+    if (k >= 1) e_cell<T>(I, c, kr, s, k, src_e, src_h, a.jx, gA, nfb, true);
+}
+
+template <typename T>
+__device__ __forceinline__ void pic_probes(PicField<T> &a, const FdtdInstance &I,
+                                           GlobalStore<T> &s, int t, int gt, int gstride, int n)
+{
+    if (gt < 2 && t >= I.probe_lo[gt] && t <= I.probe_hi[gt])
+        a.f.probe[I.probe_offset + (int64_t)t * 2 + gt] = s.Ex(I.probe_cell[gt]);
+    if (a.f.hist && I.hist_interval > 0 && t > 0 && (t % I.hist_interval) == 0) {
+        const int row = t / I.hist_interval;
+        if (row < I.hist_rows)
+            for (int k = gt; k < n; k += gstride)
+                a.f.hist[I.hist_offset + (int64_t)row * n + k] = s.Ex(k);
+    }
+}
+
+template <typename T>
+__global__ void pic_e_kernel(PicField<T> a, int t_arg)
+{
+    const FdtdInstance &I = a.f.inst[0];
+    const int t = pic_step_index(a, t_arg);
+    GlobalStore<T> s = global_store<T>(I, a.f);
+    const Scal<T> c = make_scal<T>(I);
+    Kerr<T> kr;
+    kr.setup(I);
+    const double *Exs = a.f.src + I.src_offset;
+    const T src_e = (T)(Exs[t] / I.sc);
+    const T src_h = I.tfsf ? (T)(Exs[I.n_steps + t] / I.sc) : T(0);
+    const int n = I.nz + 1;
+    T *gA = a.f.state + I.state_offset + (int64_t)FDTD_ST_A * n;
+    int nfb = 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        pic_e_cell<T>(a, I, s, c, kr, k, n, src_e, src_h, gA, &nfb);
+    if (nfb && a.f.fallbacks) atomicAdd(a.f.fallbacks, nfb);
+}
+
+template <typename T>
+__global__ void pic_h_kernel(PicField<T> a, int t_arg)
+{
+    const FdtdInstance &I = a.f.inst[0];
+    const int t = pic_step_index(a, t_arg);
+    GlobalStore<T> s = global_store<T>(I, a.f);
+    const Scal<T> c = make_scal<T>(I);
+    const T src_h = I.tfsf ? (T)(a.f.src[I.src_offset + I.n_steps + t] / I.sc) : T(0);
+    const int n = I.nz + 1;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int k = 1 + gt; k < n - 1; k += gridDim.x * blockDim.x) h_cell<T>(I, c, s, k, src_h);
+    if (gt == 0) tfsf_edge<T>(I, s, src_h);
+    pic_probes<T>(a, I, s, t, gt, gridDim.x * blockDim.x, n);
+}
+
+// Advances the device step counter after a multi-CTA field step.
+static __global__ void pic_tick_kernel(int32_t *step) { *step += 1; }
+static __global__ void pic_set_step_kernel(int32_t *step, int t) { *step = t; }
+
+// Whole field step in one CTA (grids up to PIC_FUSED_MAX cells): E phase, barrier, H phase,
+// probes, then the step counter moves on.  Saves two launches per step.
+constexpr int PIC_FUSED_MAX = 32768;
+template <typename T>
+__global__ void __launch_bounds__(1024) pic_field_fused_kernel(PicField<T> a, int32_t *step_w,
+                                                                int t_arg)
+{
+    const FdtdInstance &I = a.f.inst[0];
+    const int t = pic_step_index(a, t_arg);
+    GlobalStore<T> s = global_store<T>(I, a.f);
+    const Scal<T> c = make_scal<T>(I);
+    Kerr<T> kr;
+    kr.setup(I);
+    const double *Exs = a.f.src + I.src_offset;
+    const T src_e = (T)(Exs[t] / I.sc);
+    const T src_h = I.tfsf ? (T)(Exs[I.n_steps + t] / I.sc) : T(0);
+    const int n = I.nz + 1;
+    T *gA = a.f.state + I.state_offset + (int64_t)FDTD_ST_A * n;
+    int nfb = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
+        pic_e_cell<T>(a, I, s, c, kr, k, n, src_e, src_h, gA, &nfb);
+    __syncthreads();
+    for (int k = 1 + threadIdx.x; k < n - 1; k += blockDim.x) h_cell<T>(I, c, s, k, src_h);
+    if (threadIdx.x == 0) tfsf_edge<T>(I, s, src_h);
+    pic_probes<T>(a, I, s, t, threadIdx.x, blockDim.x, n);
+    if (nfb && a.f.fallbacks) atomicAdd(a.f.fallbacks, nfb);
+    __syncthreads();
+    if (threadIdx.x == 0 && step_w) *step_w = t + 1;
+}
+
+// ---- re-binning by cell (counting sort; order within a cell is not kept and does not matter)
+static __global__ void pic_hist_kernel(int n_part, const int32_t *cell, int32_t *counts, int nz1)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_part; p += gridDim.x * blockDim.x) {
+        const int c = cell[p];
+        if (c >= 0 && c < nz1) atomicAdd(counts + c, 1);
+    }
+}
+
+// Exclusive scan of counts[0..n) into cursor (one CTA of 1024 threads, contiguous segments).
+static __global__ void __launch_bounds__(1024) pic_scan_kernel(const int32_t *counts, int32_t *cursor, int n)
+{
+    __shared__ int part[1024];
+    const int tid = threadIdx.x;
+    const int seg = (n + blockDim.x - 1) / blockDim.x;
+    const int lo = min(n, tid * seg), hi = min(n, lo + seg);
+    int s = 0;
+    for (int i = lo; i < hi; ++i) s += counts[i];
+    part[tid] = s;
+    __syncthreads();
+    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+        const int v = (tid >= off) ? part[tid - off] : 0;
+        __syncthreads();
+        part[tid] += v;
+        __syncthreads();
+    }
+    int run = part[tid] - s;
+    for (int i = lo; i < hi; ++i) {
+        cursor[i] = run;
+        run += counts[i];
+    }
+}
+
+template <typename T>
+__global__ void pic_scatter_kernel(int n_part, const int32_t *cell, const T *frac, const T *ux,
+                                   const T *uz, const int32_t *id, int32_t *cursor, int nz1,
+                                   int32_t *cell2, T *frac2, T *ux2, T *uz2, int32_t *id2)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_part; p += gridDim.x * blockDim.x) {
+        const int c = cell[p];
+        const int q = (c >= 0 && c < nz1) ? atomicAdd(cursor + c, 1) : -1;
+        if (q < 0 || q >= n_part) continue;
+        cell2[q] = c;
+        frac2[q] = frac[p];
+        ux2[q] = ux[p];
+        uz2[q] = uz[p];
+        id2[q] = id[p];
+    }
+}
+
+template <typename T>
+__global__ void pic_finish_kernel(const T *state, int n, int32_t *status)
+{
+    bool bad = false;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        bad |= !(isfinite((double)state[k]) && isfinite((double)state[n + k]));
+    if (bad) atomicOr(status + 1, FDTD_STATUS_NONFINITE);
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Scratch layout shared by the size query and the launcher.
+struct PicScratch {
+    size_t acc, counts, cursor, step, cell2, frac2, ux2, uz2, id2, total;
+};
+inline PicScratch pic_scratch_layout(int tsize, int nz, int n_part)
+{
+    PicScratch L;
+    const size_t nz1 = (size_t)nz + 1;
+    const int W = (tsize == 8) ? 2 : 1;
+    size_t o = 0;
+    L.acc = o; o = align256(o + 2 * W * nz1 * 8);
+    L.counts = o; o = align256(o + (nz1 + 1) * 4);
+    L.cursor = o; o = align256(o + (nz1 + 1) * 4);
+    L.step = o; o = align256(o + 4);
+    L.cell2 = o; o = align256(o + (size_t)n_part * 4);
+    L.frac2 = o; o = align256(o + (size_t)n_part * tsize);
+    L.ux2 = o; o = align256(o + (size_t)n_part * tsize);
+    L.uz2 = o; o = align256(o + (size_t)n_part * tsize);
+    L.id2 = o; o = align256(o + (size_t)n_part * 4);
+    L.total = o;
+    return L;
+}
+
+// Per-kernel-type CUDA-event timing (see FdtdPicTiming in fdtdpic.h).
+struct PicTimer {
+    FdtdPicTiming *out;
+    cudaStream_t st;
+    cudaEvent_t ev[2];
+    int open;
+    float *slot;
+    void begin(float *which)
+    {
+        if (!out) return;
+        cudaEventRecord(ev[0], st);
+        slot = which;
+    }
+    void end()
+    {
+        if (!out) return;
+        cudaEventRecord(ev[1], st);
+        cudaEventSynchronize(ev[1]);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        *slot += ms;
+    }
+};
+
+template <typename T>
+struct PicPlan {
+    int threads, fblocks, pblocks, sblocks, nz1;
+    bool fused;
+    PicArgs<T> pa;
+    PicField<T> pf;
+    int32_t *counts, *cursor, *step;
+    // particle buffers: A = caller's, B = scratch
+    int32_t *cellA, *cellB, *idA, *idB;
+    T *fracA, *fracB, *uxA, *uxB, *uzA, *uzB;
+};
+
+// Enqueue one step; `sorted` selects which buffer holds the particles (flips when re-binning).
+template <typename T>
+void pic_enqueue_step(PicPlan<T> &P, const PicBeam &bm, int t, bool do_sort, bool &in_b,
+                      bool device_step, cudaStream_t st, PicTimer *tm)
+{
+    if (do_sort) {
+        int32_t *cS = in_b ? P.cellB : P.cellA, *cD = in_b ? P.cellA : P.cellB;
+        int32_t *iS = in_b ? P.idB : P.idA, *iD = in_b ? P.idA : P.idB;
+        T *fS = in_b ? P.fracB : P.fracA, *fD = in_b ? P.fracA : P.fracB;
+        T *xS = in_b ? P.uxB : P.uxA, *xD = in_b ? P.uxA : P.uxB;
+        T *zS = in_b ? P.uzB : P.uzA, *zD = in_b ? P.uzA : P.uzB;
+        if (tm) tm->begin(&tm->out->sort_ms);
+        cudaMemsetAsync(P.counts, 0, (size_t)(P.nz1 + 1) * 4, st);
+        pic_hist_kernel<<<P.sblocks, P.threads, 0, st>>>(bm.n_part, cS, P.counts, P.nz1);
+        pic_scan_kernel<<<1, 1024, 0, st>>>(P.counts, P.cursor, P.nz1);
+        pic_scatter_kernel<T><<<P.sblocks, P.threads, 0, st>>>(bm.n_part, cS, fS, xS, zS, iS,
+                                                              P.cursor, P.nz1, cD, fD, xD, zD, iD);
+        if (tm) tm->end();
+        in_b = !in_b;
+    }
+    P.pa.cell = in_b ? P.cellB : P.cellA;
+    P.pa.frac = in_b ? P.fracB : P.fracA;
+    P.pa.ux = in_b ? P.uxB : P.uxA;
+    P.pa.uz = in_b ? P.uzB : P.uzA;
+    if (bm.n_part > 0) {
+        if (tm) tm->begin(&tm->out->push_ms);
+        pic_push_kernel<T><<<P.pblocks, PIC_THREADS, 0, st>>>(P.pa);
+        if (tm) tm->end();
+    }
+    PicField<T> pf = P.pf;
+    pf.step = device_step ? P.step : nullptr;
+    if (tm) tm->begin(&tm->out->field_ms);
+    if (P.fused) {
+        pic_field_fused_kernel<T><<<1, 1024, 0, st>>>(pf, device_step ? P.step : nullptr, t);
+    } else {
+        pic_e_kernel<T><<<P.fblocks, P.threads, 0, st>>>(pf, t);
+        pic_h_kernel<T><<<P.fblocks, P.threads, 0, st>>>(pf, t);
+        if (device_step) pic_tick_kernel<<<1, 1, 0, st>>>(P.step);
+    }
+    if (tm) tm->end();
+}
+
+// Captured step blocks, kept for replay by later calls with identical arguments.
+struct PicGraphEntry {
+    unsigned char key[512];
+    size_t key_len;
+    cudaGraphExec_t exec;
+};
+PicGraphEntry *pic_graph_lookup(const void *key, size_t len);
+void pic_graph_store(const void *key, size_t len, cudaGraphExec_t exec);
+cudaStream_t pic_capture_stream();
+
+template <typename T>
+int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &fa,
+               const PicBeam &bm, int32_t *cell, T *frac, T *ux, T *uz, int32_t *id, T *jx, T *jz,
+               T *hyp, unsigned char *scratch, int32_t *status, FdtdPicTiming *timing,
+               cudaStream_t st)
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FDTDPIC_ERR_NODEV;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const PicScratch L = pic_scratch_layout(precision_bytes, h.nz, bm.n_part);
+    const int nz1 = h.nz + 1;
+    constexpr int W = Fix<T>::W;
+    PicPlan<T> P;
+    unsigned long long *acc = (unsigned long long *)(scratch + L.acc);
+    P.counts = (int32_t *)(scratch + L.counts);
+    P.cursor = (int32_t *)(scratch + L.cursor);
+    P.step = (int32_t *)(scratch + L.step);
+    P.cellA = cell; P.fracA = frac; P.uxA = ux; P.uzA = uz; P.idA = id;
+    P.cellB = (int32_t *)(scratch + L.cell2);
+    P.fracB = (T *)(scratch + L.frac2);
+    P.uxB = (T *)(scratch + L.ux2);
+    P.uzB = (T *)(scratch + L.uz2);
+    P.idB = (int32_t *)(scratch + L.id2);
+    P.nz1 = nz1;
+    P.threads = 256;
+    P.fblocks = (nz1 + P.threads - 1) / P.threads;
+    if (P.fblocks > 8 * sms) P.fblocks = 8 * sms;
+    P.fused = nz1 <= PIC_FUSED_MAX;
+    PicArgs<T> &pa = P.pa;
+    pa.n_part = bm.n_part; pa.nz = h.nz; pa.clo = bm.clo; pa.chi = bm.chi;
+    pa.chunk = bm.chunk > 0 ? bm.chunk : 1024;
+    pa.kE = (T)bm.kE; pa.kH = (T)bm.kH; pa.sc = (T)bm.sc; pa.kJ = (T)bm.kJ; pa.kJz = (T)bm.kJz;
+    pa.jscale = bm.jscale; pa.jinv = 1.0 / bm.jscale;
+    pa.jscale_f = (float)bm.jscale; pa.jinv_f = (float)(1.0 / bm.jscale);
+    const T *st0 = fa.state + h.state_offset;
+    pa.ex = st0 + (int64_t)FDTD_ST_EX * nz1;
+    pa.hy = st0 + (int64_t)FDTD_ST_HY * nz1;
+    pa.hyp = hyp;
+    pa.acc = acc;
+    pa.status = status;
+    P.pf.f = fa; P.pf.acc = acc; P.pf.jx = jx; P.pf.jz = jz; P.pf.hyp = hyp;
+    P.pf.jinv = pa.jinv; P.pf.jinv_f = pa.jinv_f; P.pf.step = nullptr;
+    P.pblocks = (bm.n_part + pa.chunk - 1) / pa.chunk;
+    P.sblocks = (bm.n_part + P.threads - 1) / P.threads;
+    if (P.sblocks > 16 * sms) P.sblocks = 16 * sms;
+    if (P.sblocks < 1) P.sblocks = 1;
+
+    cudaError_t e = cudaMemsetAsync(acc, 0, (size_t)2 * W * nz1 * 8, st);
+    if (e != cudaSuccess) return cuda_status(e);
+    if (!h.resume) fdtd_global_init_kernel<T><<<P.fblocks, P.threads, 0, st>>>(fa);
+
+    PicTimer tmr{timing, st, {nullptr, nullptr}, 0, nullptr};
+    if (timing) {
+        *timing = FdtdPicTiming{};
+        cudaEventCreate(&tmr.ev[0]);
+        cudaEventCreate(&tmr.ev[1]);
+    }
+    const bool sorting = bm.sort_every > 0 && bm.n_part > 0;
+    // one captured block = two re-binning periods, so the particles end where they started
+    const int K = sorting ? 2 * bm.sort_every : 64;
+    const int total = h.step_end - h.step_begin;
+    const int nblocks = timing ? 0 : total / K;
+    bool in_b = false;
+    int t = h.step_begin;
+    if (nblocks > 0) {
+        struct Key {
+            const void *p[16];
+            FdtdInstance inst;
+            PicBeam beam;
+            int K, sms;
+        } key;
+        memset(&key, 0, sizeof(key));
+        const void *ptrs[16] = {fa.inst, fa.src, fa.state, fa.probe, fa.hist, fa.pml_tab, cell,
+                                frac, ux, uz, id, jx, jz, hyp, scratch, status};
+        for (int i = 0; i < 16; ++i) key.p[i] = ptrs[i];
+        key.inst = h;
+        key.inst.step_begin = key.inst.step_end = key.inst.resume = 0;
+        key.beam = bm;
+        key.K = K;
+        key.sms = sms;
+        PicGraphEntry *ent = pic_graph_lookup(&key, sizeof(key));
+        cudaGraphExec_t exec = ent ? ent->exec : nullptr;
+        if (!exec) {
+            cudaStream_t cs = pic_capture_stream();
+            if (!cs) return FDTDPIC_ERR_CUDA;
+            e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return cuda_status(e);
+            bool cb = false;
+            for (int j = 0; j < K; ++j)
+                pic_enqueue_step<T>(P, bm, 0, sorting && (j % bm.sort_every) == 0, cb, true, cs,
+                                    nullptr);
+            cudaGraph_t graph = nullptr;
+            e = cudaStreamEndCapture(cs, &graph);
+            if (e != cudaSuccess) return cuda_status(e);
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_status(e);
+            pic_graph_store(&key, sizeof(key), exec);
+        }
+        pic_set_step_kernel<<<1, 1, 0, st>>>(P.step, t);
+        for (int b = 0; b < nblocks; ++b) {
+            e = cudaGraphLaunch(exec, st);
+            if (e != cudaSuccess) return cuda_status(e);
+        }
+        t += nblocks * K;
+    }
+    for (; t < h.step_end; ++t)
+        pic_enqueue_step<T>(P, bm, t, sorting && ((t - h.step_begin) % bm.sort_every) == 0, in_b,
+                            false, st, timing ? &tmr : nullptr);
+    if (in_b && bm.n_part > 0) {
+        const size_t np = (size_t)bm.n_part;
+        e = cudaMemcpyAsync(cell, P.cellB, np * 4, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(frac, P.fracB, np * sizeof(T), cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ux, P.uxB, np * sizeof(T), cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(uz, P.uzB, np * sizeof(T), cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(id, P.idB, np * 4, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    pic_finish_kernel<T><<<P.fblocks, P.threads, 0, st>>>(fa.state + h.state_offset, nz1, status);
+    if (timing) {
+        timing->steps = total;
+        cudaEventDestroy(tmr.ev[0]);
+        cudaEventDestroy(tmr.ev[1]);
+    }
+    return cuda_status(cudaGetLastError());
+}
+
+}  // namespace fdtdpic

@@ -25,7 +25,8 @@ UNITS = {
     "capi.cu": [],
     "fdtd1d_f64.cu": ["-fmad=false"],
     "fdtd1d_f32.cu": [],
-    "pic.cu": [],
+    "pic_f64.cu": ["-fmad=false"],
+    "pic_f32.cu": [],
     "dft.cu": [],
     "noalloc.cu": [],
 }
@@ -134,6 +135,12 @@ def _declare(L):
     L.fdtd1d_run_global.argtypes = [c_int] + [P] * 9 + [P]
     L.fdtdpic_cubic_root0.restype = c_int
     L.fdtdpic_cubic_root0.argtypes = [c_int, P, P, P]
+    L.fdtdpic_scratch_bytes.restype = c_i64
+    L.fdtdpic_scratch_bytes.argtypes = [c_int, c_int, c_int]
+    L.fdtdpic_pic_jscale.restype = ctypes.c_double
+    L.fdtdpic_pic_jscale.argtypes = [P]
+    L.fdtdpic_run.restype = c_int
+    L.fdtdpic_run.argtypes = [c_int] + [P] * 16 + [c_i64, P, P, P]
     for name, argt in _EXTRA_DECLS.items():
         if hasattr(L, name):
             fn = getattr(L, name)

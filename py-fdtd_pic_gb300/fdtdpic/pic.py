@@ -1,0 +1,168 @@
+"""Electron-beam PIC coupled to one grid, on the GPU (``fdtdpic_run`` in the C ABI).
+
+The reference leaves its ``Jx`` hook (MasterController.py:93,159; BaseFDTD11.py:667) empty; this
+module fills it with a beam of macroparticles.  Positions are an int32 cell plus a fraction in
+[0, 1) (units of dz), momenta are u/c = gamma v / c.  See include/fdtdpic.h for the step.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from ._lib import F32, F64, INSTANCE_DTYPE, ST, STATE_ARRAYS, check, lib
+from .engine import _dtype, _ptr, _require_cuda
+from .grid import Grid, pack
+
+C0 = 299792458.0
+Q_E = -1.602176634e-19
+M_E = 9.1093837139e-31
+
+
+class FdtdPicTiming(ctypes.Structure):
+    _fields_ = [("push_ms", ctypes.c_float), ("field_ms", ctypes.c_float),
+                ("sort_ms", ctypes.c_float), ("steps", ctypes.c_int32)]
+
+
+class PicBeam(ctypes.Structure):
+    _fields_ = [("n_part", ctypes.c_int32), ("clo", ctypes.c_int32), ("chi", ctypes.c_int32),
+                ("sort_every", ctypes.c_int32), ("chunk", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("kE", ctypes.c_double), ("kH", ctypes.c_double),
+                ("sc", ctypes.c_double), ("kJ", ctypes.c_double), ("kJz", ctypes.c_double),
+                ("jscale", ctypes.c_double)]
+
+
+@dataclass
+class Beam:
+    """Host copy of a beam: (cell, frac, ux, uz, id) plus its domain and macro-weight."""
+    cell: np.ndarray
+    frac: np.ndarray
+    ux: np.ndarray
+    uz: np.ndarray
+    id: np.ndarray
+    clo: int
+    chi: int
+    weight: float  # electrons per unit area per macroparticle [m^-2]
+
+    @property
+    def n(self):
+        return len(self.cell)
+
+
+def make_beam(n_part, clo, chi, dz, density=1e14, v_mean=0.3, v_spread=0.003, seed=20261203):
+    """Seeded beam: positions uniform over cells [clo, chi), vz ~ N(v_mean c, v_spread c),
+    vx = 0, equal weights giving ``density`` [m^-3]; sorted by position."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    zeta = clo + (chi - clo) * rng.random(n_part)
+    vz = rng.normal(v_mean, v_spread, n_part)
+    uz = vz / np.sqrt(1.0 - vz * vz)
+    order = np.argsort(zeta, kind="stable")
+    zeta, uz = zeta[order], uz[order]
+    cell = np.floor(zeta).astype(np.int32)
+    weight = density * (chi - clo) * dz / max(1, n_part)
+    return Beam(cell=cell, frac=zeta - cell, ux=np.zeros(n_part), uz=uz.copy(),
+                id=np.arange(n_part, dtype=np.int32), clo=int(clo), chi=int(chi), weight=weight)
+
+
+def beam_constants(dz, dt, weight, mu0, q=Q_E, m=M_E):
+    """(kE, kH, sc, kJ, kJz) of the Boris step and deposit, momentum in units of c."""
+    return dict(kE=q * dt / (2.0 * m * C0), kH=-q * mu0 * dt / (2.0 * m), sc=C0 * dt / dz,
+                kJ=q * weight * C0, kJz=q * weight * dz / dt)
+
+
+class PicRun:
+    """One grid plus a beam, resident on the GPU; ``step(n)`` advances n steps."""
+
+    def __init__(self, grid: Grid, beam: Beam, dz: float, dt: float, mu0: float,
+                 precision="f32", sort_every=32, chunk=0, device=None):
+        _require_cuda()
+        self.L = lib()
+        self.prec, self.tdt = _dtype(precision)
+        dev = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+        self.dev = dev
+        self.grid = grid
+        g = grid
+        pk = pack([g], 8 if self.prec == F64 else 4)
+        self.desc = pk["desc"]
+        self.d_desc = torch.from_numpy(self.desc.view(np.uint8).copy()).to(dev)
+        self.d_table = torch.from_numpy(pk["table"]).to(dev)
+        self.d_src = torch.from_numpy(pk["src"]).to(dev)
+        self.d_state = torch.zeros(pk["n_state"], dtype=self.tdt, device=dev)
+        self.d_probe = torch.zeros(pk["n_probe"], dtype=self.tdt, device=dev)
+        n = g.nz + 1
+        self.d_hyp = torch.zeros(n, dtype=self.tdt, device=dev)
+        self.d_jx = torch.zeros(n, dtype=self.tdt, device=dev)
+        self.d_jz = torch.zeros(n, dtype=self.tdt, device=dev)
+        self.d_status = torch.zeros(2, dtype=torch.int32, device=dev)
+        self.beam = beam
+        self.d_cell = torch.from_numpy(np.ascontiguousarray(beam.cell, np.int32)).to(dev)
+        self.d_frac = torch.from_numpy(np.ascontiguousarray(beam.frac)).to(dev, self.tdt)
+        self.d_ux = torch.from_numpy(np.ascontiguousarray(beam.ux)).to(dev, self.tdt)
+        self.d_uz = torch.from_numpy(np.ascontiguousarray(beam.uz)).to(dev, self.tdt)
+        self.d_id = torch.from_numpy(np.ascontiguousarray(beam.id, np.int32)).to(dev)
+        self.pb = PicBeam()
+        self.pb.n_part, self.pb.clo, self.pb.chi = beam.n, beam.clo, beam.chi
+        self.pb.sort_every, self.pb.chunk = sort_every, chunk
+        self.constants = beam_constants(dz, dt, beam.weight, mu0)
+        for name, v in self.constants.items():
+            setattr(self.pb, name, v)
+        self.pb.jscale = self.L.fdtdpic_pic_jscale(ctypes.byref(self.pb))
+        self.scratch_bytes = int(self.L.fdtdpic_scratch_bytes(self.prec, g.nz, beam.n))
+        self.d_scratch = torch.zeros(max(1, self.scratch_bytes), dtype=torch.uint8, device=dev)
+        self.step_done = 0
+
+    def step(self, n_steps, stream=None, timing=None):
+        """Enqueue the next n_steps steps (asynchronous unless ``timing`` is given: then the
+        call runs launch by launch and fills the FdtdPicTiming with per-kernel GPU time)."""
+        g = self.grid
+        t0 = self.step_done
+        t1 = min(g.n_steps, t0 + n_steps)
+        d = self.desc.copy()
+        d["step_begin"], d["step_end"] = t0, t1
+        d["resume"] = 1 if t0 > 0 else 0
+        self.d_desc.copy_(torch.from_numpy(d.view(np.uint8).copy()).to(self.dev), non_blocking=False)
+        st = ctypes.c_void_p((stream or torch.cuda.current_stream()).cuda_stream)
+        check(self.L.fdtdpic_run(
+            self.prec, d.ctypes.data, _ptr(self.d_desc), _ptr(self.d_table), _ptr(self.d_src),
+            _ptr(self.d_state), _ptr(self.d_probe), ctypes.byref(self.pb), _ptr(self.d_cell),
+            _ptr(self.d_frac), _ptr(self.d_ux), _ptr(self.d_uz), _ptr(self.d_id),
+            _ptr(self.d_jx), _ptr(self.d_jz), _ptr(self.d_hyp), _ptr(self.d_scratch),
+            self.scratch_bytes, _ptr(self.d_status),
+            ctypes.byref(timing) if timing is not None else None, st), "fdtdpic_run")
+        self.step_done = t1
+
+    def reset(self, beam: Beam | None = None):
+        """Back to step 0 with the initial beam (device-to-device; for repeated runs)."""
+        b = self.beam if beam is None else beam
+        self.d_cell.copy_(torch.from_numpy(np.ascontiguousarray(b.cell, np.int32)))
+        self.d_frac.copy_(torch.from_numpy(np.ascontiguousarray(b.frac)))
+        self.d_ux.copy_(torch.from_numpy(np.ascontiguousarray(b.ux)))
+        self.d_uz.copy_(torch.from_numpy(np.ascontiguousarray(b.uz)))
+        self.d_id.copy_(torch.from_numpy(np.ascontiguousarray(b.id, np.int32)))
+        self.d_hyp.zero_()
+        self.d_probe.zero_()
+        self.d_status.zero_()
+        self.step_done = 0
+
+    def fields(self):
+        n = self.grid.nz + 1
+        s = self.d_state.double().cpu().numpy()
+        return {k: s[v * n:(v + 1) * n].copy() for k, v in ST.items()}
+
+    def particles(self):
+        """Host copy ordered by particle id: (cell, frac, ux, uz)."""
+        idx = self.d_id.cpu().numpy()
+        order = np.argsort(idx)
+        return (self.d_cell.cpu().numpy()[order], self.d_frac.double().cpu().numpy()[order],
+                self.d_ux.double().cpu().numpy()[order], self.d_uz.double().cpu().numpy()[order])
+
+    def probes(self):
+        return self.d_probe.double().cpu().numpy().reshape(self.grid.n_steps, 2)
+
+    def currents(self):
+        return self.d_jx.double().cpu().numpy(), self.d_jz.double().cpu().numpy()
+
+    def status(self):
+        return self.d_status.cpu().numpy()

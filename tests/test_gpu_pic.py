@@ -1,0 +1,129 @@
+"""GPU PIC (fdtdpic_run through the C ABI) against the FP64 CPU oracle's beam model."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+NZ, T, NPART = 512, 600, 20000
+DZ = 0.015
+DT = 0.5 * DZ / O.C0
+CLO, CHI = 40, 480
+
+
+def _torch():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _case(precision, sort_every=32, chunk=0, steps=(T,)):
+    torch = _torch()
+    import scipy.constants as sc
+    from fdtdpic.grid import lorentz_kerr_grid
+    from fdtdpic.pic import PicRun, make_beam
+    g = lorentz_kerr_grid(NZ, T, front=300, rear=400, nzsrc=60, probes=(50, 350), chi3=1e-2)
+    beam = make_beam(NPART, CLO, CHI, DZ)
+    run = PicRun(g, beam, DZ, DT, sc.mu_0, precision=precision, sort_every=sort_every, chunk=chunk)
+    snaps = []
+    for s in steps:
+        run.step(s)
+        torch.cuda.synchronize()
+        snaps.append((run.fields(), run.particles(), run.currents()))
+    return g, beam, run, snaps
+
+
+def _oracle(g, beam, n_steps=T):
+    import scipy.constants as sc
+    P = O.RefParams(Nz=NZ, timeSteps=T, dz=DZ, delT=DT, courantNo=O.f32(0.5),
+                    materialFrontEdge=300, materialRearEdge=400, pmlWidth=20, nzsrc=60,
+                    freq_in=1e9, permit_0=g.eps0, permea_0=sc.mu_0, nonLinMed=True,
+                    FreeSpace=False, plasmaFreqE=np.sqrt(2.0) * 2 * np.pi * 1.5e9,
+                    omega_0E=2 * np.pi * 1.5e9, gammaE=2 * np.pi * 0.1e9, chi3Stat=1e-2,
+                    sigmaOpt=O.sigma_opt(DZ, g.eps0, sc.mu_0))
+    cell, frac = beam.cell.copy(), beam.frac.copy()
+    ux, uz = beam.ux.copy(), beam.uz.copy()
+    k = O.pic_constants(DZ, DT, beam.weight, sc.mu_0)
+    r = O.integrate_pic(P, O.KERR, g.exs, np.zeros(T), cell, frac, ux, uz, k, CLO, CHI,
+                        n_steps=n_steps, probe_cells=(50, 350))
+    return r, (cell, frac, ux, uz)
+
+
+def _zeta(cell, frac):
+    return cell + frac
+
+
+def test_pic_fp64_matches_oracle():
+    g, beam, run, snaps = _case("f64")
+    f, (cell, frac, ux, uz), (jx, jz) = snaps[-1]
+    r, (oc, of, oux, ouz) = _oracle(g, beam)
+    assert run.status()[0] == 0 and r["lost"] == 0
+    for key, want in (("Ex", r["Ex"]), ("Hy", r["Hy"]), ("Dx", r["Dx"])):
+        assert O.rel_l2(f[key], want) <= 1e-12, key
+    assert O.rel_l2(run.probes()[:, 1], r["probes"][:, 1]) <= 1e-12
+    assert O.rel_l2(jx, r["Jx"]) <= 1e-11
+    assert O.rel_l2(jz, r["Jz"]) <= 1e-12
+    assert np.array_equal(cell, oc)
+    assert np.abs(frac - of).max() <= 1e-12
+    assert O.rel_l2(ux, oux) <= 1e-11
+    assert O.rel_l2(uz, ouz) <= 1e-14
+
+
+def test_pic_fp32_error_vs_fp64_oracle():
+    g, beam, run, snaps = _case("f32")
+    f, (cell, frac, ux, uz), (jx, jz) = snaps[-1]
+    r, (oc, of, oux, ouz) = _oracle(g, beam)
+    assert run.status()[0] == 0
+    # stated FP32 bounds against the FP64 oracle after 600 coupled steps
+    assert O.rel_l2(f["Ex"], r["Ex"]) <= 1e-4
+    assert O.rel_l2(f["Hy"], r["Hy"]) <= 1e-4
+    assert O.rel_l2(run.probes()[:, 1], r["probes"][:, 1]) <= 1e-4
+    assert np.abs(_zeta(cell, frac) - _zeta(oc, of)).max() <= 1e-3
+    assert O.rel_l2(ux, oux) <= 1e-3
+    assert O.rel_l2(uz, ouz) <= 1e-6
+
+
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_pic_run_to_run_bit_stable(precision):
+    _, _, run1, s1 = _case(precision, sort_every=16)
+    _, _, run2, s2 = _case(precision, sort_every=16)
+    for k in ("Ex", "Hy", "Dx"):
+        np.testing.assert_array_equal(s1[-1][0][k], s2[-1][0][k])
+    for a, b in zip(s1[-1][1], s2[-1][1]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(s1[-1][2][0], s2[-1][2][0])
+
+
+def test_pic_result_independent_of_binning_and_chunking():
+    """Deposits are exact integer sums: re-binning cadence and CTA chunking change nothing."""
+    _, _, _, a = _case("f32", sort_every=0, chunk=512)
+    _, _, _, b = _case("f32", sort_every=7, chunk=2048)
+    np.testing.assert_array_equal(a[-1][0]["Ex"], b[-1][0]["Ex"])
+    np.testing.assert_array_equal(a[-1][2][0], b[-1][2][0])
+    for x, y in zip(a[-1][1], b[-1][1]):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_pic_resume_in_chunks_equals_one_call():
+    _, _, _, whole = _case("f64", steps=(T,))
+    _, _, _, parts = _case("f64", steps=(250, 200, 150))
+    for k in ("Ex", "Hy", "Dx"):
+        np.testing.assert_array_equal(whole[-1][0][k], parts[-1][0][k])
+
+
+def test_pic_gpu_jz_conserves_charge():
+    g, beam, run, snaps = _case("f64", steps=(T - 1, 1))
+    (_, (c0, f0, _, _), _), (_, (c1, f1, _, _), (jx, jz)) = snaps
+    qw = O.Q_E * beam.weight
+
+    def charge(c, f):
+        Q = np.zeros(NZ + 1)
+        np.add.at(Q, c, qw * (1 - f))
+        np.add.at(Q, c + 1, qw * f)
+        return Q
+
+    h = np.arange(CLO + 2, CHI - 2)
+    resid = (charge(c1, f1)[h] - charge(c0, f0)[h]) / DT + (jz[h] - jz[h - 1]) / DZ
+    assert np.abs(resid).max() <= 1e-9 * np.abs(jz).max() / DZ
