@@ -212,6 +212,21 @@ int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d
                 int64_t scratch_bytes, int32_t *d_status, FdtdPicTiming *timing,
                 fdtdpic_stream_t stream);
 
+/* fdtdpic_run for callers that cannot allocate device memory (no counterpart in the
+ * reference; the reference allocates nothing on a device).  For example code running inside
+ * another framework's memory pool, or a plug-in in a host that has reserved the whole device.
+ * Same arguments minus the scratch: it uses a 24 MiB array compiled into the library, held on
+ * every device that loads the library until exit.  Runs needing more scratch than that
+ * (fdtdpic_scratch_bytes > 24 MiB) return FDTDPIC_ERR_OOM.  All calls share the array, so calls
+ * that overlap on the GPU race: serialise them.  The first call on a device looks up the array's
+ * address (make it before any stream capture).  Launches kernel by kernel; no cudaMalloc, no
+ * graph capture, no event or stream creation. */
+int fdtdpic_run_noalloc(int precision, const FdtdInstance *h_inst, const FdtdInstance *d_inst,
+                        const double *d_pml_tab, const double *d_src, void *d_state, void *d_probe,
+                        const PicBeam *beam, int32_t *d_cell, void *d_frac, void *d_ux,
+                        void *d_uz, int32_t *d_id, void *d_jx, void *d_jz, void *d_hyp,
+                        int32_t *d_status, fdtdpic_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,11 +27,11 @@ int run_cubic_root0(int n, const double *coef, double *out, cudaStream_t st);
 int run_pic_f64(const FdtdInstance &h, const BatchArgs<double> &fa, const PicBeam &bm,
                 int32_t *cell, double *frac, double *ux, double *uz, int32_t *id, double *jx,
                 double *jz, double *hyp, unsigned char *scratch, int32_t *status,
-                FdtdPicTiming *timing, cudaStream_t st);
+                FdtdPicTiming *timing, cudaStream_t st, bool allow_graphs = true);
 int run_pic_f32(const FdtdInstance &h, const BatchArgs<float> &fa, const PicBeam &bm,
                 int32_t *cell, float *frac, float *ux, float *uz, int32_t *id, float *jx,
                 float *jz, float *hyp, unsigned char *scratch, int32_t *status,
-                FdtdPicTiming *timing, cudaStream_t st);
+                FdtdPicTiming *timing, cudaStream_t st, bool allow_graphs = true);
 
 // ---- captured PIC step blocks (replayed by calls with identical arguments) -------------
 static PicGraphEntry g_graphs[16];
@@ -69,7 +69,7 @@ cudaStream_t pic_capture_stream()
     return streams[dev];
 }
 
-static int check_instance(const FdtdInstance &I)
+int check_instance(const FdtdInstance &I)
 {
     if (I.nz < 2 || I.n_steps < 0 || I.step_begin < 0 || I.step_end < I.step_begin ||
         I.step_end > I.n_steps)

@@ -6,9 +6,10 @@ namespace fdtdpic {
 int run_pic_f32(const FdtdInstance &h, const BatchArgs<float> &fa, const PicBeam &bm,
                 int32_t *cell, float *frac, float *ux, float *uz, int32_t *id, float *jx,
                 float *jz, float *hyp, unsigned char *scratch, int32_t *status, FdtdPicTiming *timing,
-                cudaStream_t st)
+                cudaStream_t st, bool allow_graphs)
 {
-    return launch_pic<float>(4, h, fa, bm, cell, frac, ux, uz, id, jx, jz, hyp, scratch, status, timing, st);
+    return launch_pic<float>(4, h, fa, bm, cell, frac, ux, uz, id, jx, jz, hyp, scratch, status, timing, st,
+                          allow_graphs);
 }
 
 }  // namespace fdtdpic

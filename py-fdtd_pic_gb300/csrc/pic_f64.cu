@@ -6,9 +6,10 @@ namespace fdtdpic {
 int run_pic_f64(const FdtdInstance &h, const BatchArgs<double> &fa, const PicBeam &bm,
                 int32_t *cell, double *frac, double *ux, double *uz, int32_t *id, double *jx,
                 double *jz, double *hyp, unsigned char *scratch, int32_t *status, FdtdPicTiming *timing,
-                cudaStream_t st)
+                cudaStream_t st, bool allow_graphs)
 {
-    return launch_pic<double>(8, h, fa, bm, cell, frac, ux, uz, id, jx, jz, hyp, scratch, status, timing, st);
+    return launch_pic<double>(8, h, fa, bm, cell, frac, ux, uz, id, jx, jz, hyp, scratch, status, timing, st,
+                          allow_graphs);
 }
 
 }  // namespace fdtdpic

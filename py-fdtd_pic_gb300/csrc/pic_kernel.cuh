@@ -494,7 +494,7 @@ template <typename T>
 int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &fa,
                const PicBeam &bm, int32_t *cell, T *frac, T *ux, T *uz, int32_t *id, T *jx, T *jz,
                T *hyp, unsigned char *scratch, int32_t *status, FdtdPicTiming *timing,
-               cudaStream_t st)
+               cudaStream_t st, bool allow_graphs = true)
 {
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return FDTDPIC_ERR_NODEV;
@@ -551,7 +551,7 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
     // one captured block = two re-binning periods, so the particles end where they started
     const int K = sorting ? 2 * bm.sort_every : 64;
     const int total = h.step_end - h.step_begin;
-    const int nblocks = timing ? 0 : total / K;
+    const int nblocks = (timing || !allow_graphs) ? 0 : total / K;
     bool in_b = false;
     int t = h.step_begin;
     if (nblocks > 0) {

@@ -141,6 +141,8 @@ def _declare(L):
     L.fdtdpic_pic_jscale.argtypes = [P]
     L.fdtdpic_run.restype = c_int
     L.fdtdpic_run.argtypes = [c_int] + [P] * 16 + [c_i64, P, P, P]
+    L.fdtdpic_run_noalloc.restype = c_int
+    L.fdtdpic_run_noalloc.argtypes = [c_int] + [P] * 17
     for name, argt in _EXTRA_DECLS.items():
         if hasattr(L, name):
             fn = getattr(L, name)
