@@ -53,6 +53,8 @@ typedef struct CUstream_st *fdtdpic_stream_t; /* == cudaStream_t */
 /* Per-instance status bits (d_status[i]) */
 #define FDTD_STATUS_NONFINITE 1 /* Ex or Hy not finite at the end of the call */
 #define FDTD_STATUS_SKIPPED 2   /* instance larger than smem_bytes: not run */
+#define FDTD_STATUS_TIMEOUT 4   /* beam step, tiled path: a bounded wait gave up */
+#define FDTD_STATUS_OVERFLOW 8  /* beam step, tiled path: a tile or migrant buffer overflowed */
 
 /* PML coefficient table: per instance FDTD_TAB_ROWS rows x (2*pml+1) columns of doubles.
  * Column c <= pml is cell c; column c > pml is cell nz+1-pml+(c-pml-1). */
@@ -172,7 +174,7 @@ typedef struct PicBeam {
     int32_t clo, chi;   /* periodic beam domain, cells [clo, chi); 2 <= clo < chi <= nz-2 */
     int32_t sort_every; /* re-bin by cell every this many steps (0: never) */
     int32_t chunk;      /* particles per CTA in the push kernel (0: library default) */
-    int32_t reserved;
+    int32_t path;       /* 0: automatic, 1: streaming kernels, 2: persistent tiled kernel */
     double kE;     /* q dt / (2 m c) */
     double kH;     /* -q mu0 dt / (2 m) */
     double sc;     /* c dt / dz */
@@ -189,10 +191,16 @@ typedef struct FdtdPicTiming {
     float field_ms; /* field step (E and H phases) */
     float sort_ms;  /* re-binning by cell */
     int32_t steps;
+    int32_t path;   /* 1: streaming kernels, 2: persistent tiled kernel (push_ms = whole kernel) */
 } FdtdPicTiming;
 
 /* Bytes of caller scratch fdtdpic_run needs (deposit accumulators, re-binning buffers). */
 int64_t fdtdpic_scratch_bytes(int precision, int nz, int n_part);
+/* Bytes of scratch with which fdtdpic_run can take the persistent tiled path for this run on the
+ * current device (the streaming requirement when that path does not apply).  The tiled path
+ * applies when the grid splits into at least two tiles of >= max(pml+2, 8) cells, one per SM;
+ * fdtdpic_run takes it whenever beam->path allows and scratch_bytes covers it. */
+int64_t fdtdpic_pic_scratch_bytes(int precision, const FdtdInstance *inst, const PicBeam *beam);
 /* The largest power-of-two scale for which no deposit accumulator can overflow. */
 double fdtdpic_pic_jscale(const PicBeam *beam);
 

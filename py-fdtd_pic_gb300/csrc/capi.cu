@@ -6,6 +6,7 @@
 
 #include "fdtd1d_launch.cuh"
 #include "pic_kernel.cuh"
+#include "pic_tiled.cuh"
 
 namespace fdtdpic {
 
@@ -32,6 +33,26 @@ int run_pic_f32(const FdtdInstance &h, const BatchArgs<float> &fa, const PicBeam
                 int32_t *cell, float *frac, float *ux, float *uz, int32_t *id, float *jx,
                 float *jz, float *hyp, unsigned char *scratch, int32_t *status,
                 FdtdPicTiming *timing, cudaStream_t st, bool allow_graphs = true);
+
+int run_pic_tiled_f64(const FdtdInstance &h, const BatchArgs<double> &fa, const PicBeam &bm,
+                      const TileGeom &g, int32_t *cell, double *frac, double *ux, double *uz,
+                      int32_t *id, double *jx, double *jz, double *hyp, unsigned char *scratch,
+                      int32_t *status, FdtdPicTiming *timing, cudaStream_t st);
+int run_pic_tiled_f32(const FdtdInstance &h, const BatchArgs<float> &fa, const PicBeam &bm,
+                      const TileGeom &g, int32_t *cell, float *frac, float *ux, float *uz,
+                      int32_t *id, float *jx, float *jz, float *hyp, unsigned char *scratch,
+                      int32_t *status, FdtdPicTiming *timing, cudaStream_t st);
+
+// Tiling of a beam run on the current device, or ok=false when the tiled path does not apply.
+static TileGeom tiled_geometry(const FdtdInstance &h, const PicBeam &b)
+{
+    TileGeom g{};
+    int dev = 0, sms = 0;
+    if (b.path == 1 || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return g;
+    return tile_geometry(h, b, sms);
+}
 
 // ---- captured PIC step blocks (replayed by calls with identical arguments) -------------
 static PicGraphEntry g_graphs[16];
@@ -226,6 +247,19 @@ double fdtdpic_pic_jscale(const PicBeam *bm)
     return ldexp(1.0, S);
 }
 
+int64_t fdtdpic_pic_scratch_bytes(int precision, const FdtdInstance *inst, const PicBeam *beam)
+{
+    if (!inst || !beam || (precision != FDTDPIC_F64 && precision != FDTDPIC_F32)) return 0;
+    if (check_instance(*inst) != FDTDPIC_OK) return 0;
+    int64_t need = fdtdpic_scratch_bytes(precision, inst->nz, beam->n_part);
+    const TileGeom tg = tiled_geometry(*inst, *beam);
+    if (tg.ok) {
+        const int64_t t = (int64_t)tile_scratch_layout(precision, tg).total;
+        if (beam->path == 2 || t > need) need = (beam->path == 2) ? t : (t > need ? t : need);
+    }
+    return need;
+}
+
 int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d_inst,
                 const double *d_pml_tab, const double *d_src, void *d_state, void *d_probe,
                 const PicBeam *beam, int32_t *d_cell, void *d_frac, void *d_ux, void *d_uz,
@@ -239,14 +273,33 @@ int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d
     int rc = check_instance(*h_inst);
     if (rc != FDTDPIC_OK) return rc;
     const PicBeam &b = *beam;
+    // |cell displacement| per step < sc must stay below one cell for the Jz deposit
     if (b.n_part < 0 || b.clo < 2 || b.chi <= b.clo || b.chi > h_inst->nz - 2 || b.sort_every < 0 ||
-        b.chunk < 0 || !(b.jscale > 0.0))
+        b.chunk < 0 || !(b.jscale > 0.0) || !(b.sc > 0.0 && b.sc < 1.0))
         return FDTDPIC_ERR_ARG;
     if (b.n_part > 0 && (!d_cell || !d_frac || !d_ux || !d_uz || !d_id)) return FDTDPIC_ERR_ARG;
     if (precision != FDTDPIC_F64 && precision != FDTDPIC_F32) return FDTDPIC_ERR_ARG;
-    if (scratch_bytes < fdtdpic_scratch_bytes(precision, h_inst->nz, b.n_part)) return FDTDPIC_ERR_OOM;
+    if (b.path < 0 || b.path > 2) return FDTDPIC_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     unsigned char *scr = (unsigned char *)d_scratch;
+    const TileGeom tg = tiled_geometry(*h_inst, b);
+    const int64_t tiled_need = tg.ok ? (int64_t)tile_scratch_layout(precision, tg).total : -1;
+    if (tg.ok && scratch_bytes >= tiled_need) {
+        if (precision == FDTDPIC_F64) {
+            BatchArgs<double> a{1, d_inst, nullptr, d_pml_tab, d_src, (double *)d_state,
+                                (double *)d_probe, nullptr, nullptr, nullptr, nullptr, 0};
+            return run_pic_tiled_f64(*h_inst, a, b, tg, d_cell, (double *)d_frac, (double *)d_ux,
+                                     (double *)d_uz, d_id, (double *)d_jx, (double *)d_jz,
+                                     (double *)d_hyp, scr, d_status, timing, st);
+        }
+        BatchArgs<float> a{1, d_inst, nullptr, d_pml_tab, d_src, (float *)d_state,
+                           (float *)d_probe, nullptr, nullptr, nullptr, nullptr, 0};
+        return run_pic_tiled_f32(*h_inst, a, b, tg, d_cell, (float *)d_frac, (float *)d_ux,
+                                 (float *)d_uz, d_id, (float *)d_jx, (float *)d_jz,
+                                 (float *)d_hyp, scr, d_status, timing, st);
+    }
+    if (b.path == 2) return tg.ok ? FDTDPIC_ERR_OOM : FDTDPIC_ERR_ARG;
+    if (scratch_bytes < fdtdpic_scratch_bytes(precision, h_inst->nz, b.n_part)) return FDTDPIC_ERR_OOM;
     if (precision == FDTDPIC_F64) {
         BatchArgs<double> a{1, d_inst, nullptr, d_pml_tab, d_src, (double *)d_state,
                             (double *)d_probe, nullptr, nullptr, nullptr, nullptr, 0};

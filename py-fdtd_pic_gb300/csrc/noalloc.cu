@@ -78,7 +78,7 @@ extern "C" int fdtdpic_run_noalloc(int precision, const FdtdInstance *h_inst,
     if (rc != FDTDPIC_OK) return rc;
     const PicBeam &b = *beam;
     if (b.n_part < 0 || b.clo < 2 || b.chi <= b.clo || b.chi > h_inst->nz - 2 || b.sort_every < 0 ||
-        b.chunk < 0 || !(b.jscale > 0.0))
+        b.chunk < 0 || !(b.jscale > 0.0) || !(b.sc > 0.0 && b.sc < 1.0))
         return FDTDPIC_ERR_ARG;
     if (b.n_part > 0 && (!d_cell || !d_frac || !d_ux || !d_uz || !d_id)) return FDTDPIC_ERR_ARG;
     if (precision != FDTDPIC_F64 && precision != FDTDPIC_F32) return FDTDPIC_ERR_ARG;

@@ -29,13 +29,37 @@ struct Fix;
 template <>
 struct Fix<float> {
     static constexpr int W = 1;
-    __device__ static void split(float v, double scale, float scale_f, long long *w)
+    // x = v * 2^S rounded to an integer using 32-bit conversions only (the 64-bit ones run on
+    // the narrow FP64 pipe).  |x| < 2^31: one conversion.  Otherwise x is a multiple of 2^8 or
+    // more, so x - floor(x / 2^32) * 2^32 is exact in float and fits an unsigned 32-bit integer.
+    __device__ static void split(float v, double, float scale_f, long long *w)
     {
-        w[0] = __float2ll_rn(v * scale_f);
+        const float x = v * scale_f;
+        if (fabsf(x) < 2147483648.f) {
+            w[0] = (long long)__float2int_rn(x);
+        } else {
+            const float h = floorf(x * 2.3283064365386963e-10f);  // 2^-32
+            const float r = fmaf(-h, 4294967296.f, x);               // exact
+            w[0] = (long long)((unsigned long long)(long long)__float2int_rn(h) << 32) +
+                   (long long)__float2uint_rn(r);
+        }
     }
-    __device__ static float join(const unsigned long long *w, double inv, float inv_f)
+    __device__ static float to_float(unsigned long long u, float inv_f)
     {
-        return __ll2float_rn((long long)w[0]) * inv_f;
+        const long long v = (long long)u;
+        const int hi = (int)(v >> 32);
+        const unsigned lo = (unsigned)(v & 0xffffffffull);
+        return fmaf((float)hi, 4294967296.f, (float)lo) * inv_f;
+    }
+    __device__ static float join(const unsigned long long *w, double, float inv_f)
+    {
+        return to_float(w[0], inv_f);
+    }
+    // words at base[w*stride + l]
+    __device__ static float join2(const unsigned long long *base, size_t, int l, double,
+                                  float inv_f)
+    {
+        return to_float(base[l], inv_f);
     }
 };
 template <>
@@ -52,6 +76,12 @@ struct Fix<double> {
     {
         return (double)(long long)w[0] * inv + (double)(long long)w[1] * (inv * (1.0 / 1099511627776.0));
     }
+    __device__ static double join2(const unsigned long long *base, size_t stride, int l, double inv,
+                                   float)
+    {
+        return (double)(long long)base[l] * inv +
+               (double)(long long)base[stride + l] * (inv * (1.0 / 1099511627776.0));
+    }
 };
 
 template <typename T>
@@ -65,7 +95,90 @@ struct PicArgs {
     const T *ex, *hy, *hyp;
     unsigned long long *acc;  // [2*W][nz+1]: Jx words then Jz words
     int32_t *status;
+    int deposit_jz;  // Jz (a diagnostic: no field uses it) only on the call's last step
 };
+
+// One particle's step (everything but the wrap), shared by the streaming and tiled kernels.
+// FP64 keeps the oracle's operation order (divisions by gamma); FP32 uses rsqrt/fast-divide.
+template <typename T>
+struct Moved {
+    int c1;       // new cell before the periodic wrap
+    T f1, ux, uz; // new fraction and momenta
+    int nx0;      // Jx nodes nx0, nx0+1 (CIC at the half-step midpoint)
+    T jx0, jx1;
+    int nzA, nzB; // Jz half nodes (nzB < 0 when the particle stays in its cell)
+    T jzA, jzB;
+};
+
+template <typename T>
+__device__ __forceinline__ void particle_step(T E, T H, int c, T f, T ux, T uz, T kE, T kH, T sc,
+                                              T kJ, T kJz, Moved<T> &m)
+{
+    const T uxm = (sizeof(T) == 8) ? ux + kE * E : (T)fmaf((float)kE, (float)E, (float)ux);
+    const T uzm = uz;
+    T uxn, uzn, dz, jxv;
+    if constexpr (sizeof(T) == 8) {
+        const T gm = sqrt(T(1) + uxm * uxm + uzm * uzm);
+        const T ty = kH * H / gm;
+        const T sy = T(2) * ty / (T(1) + ty * ty);
+        const T uxp = uxm - uzm * ty;
+        const T uzp = uzm + uxm * ty;
+        uxn = (uxm - uzp * sy) + kE * E;
+        uzn = uzm + uxp * sy;
+        const T g = sqrt(T(1) + uxn * uxn + uzn * uzn);
+        dz = sc * uzn / g;
+        jxv = kJ * uxn / g;
+    } else {
+        // fused operations written out (fmaf), so the rounding does not depend on how the
+        // compiler contracts this code in each kernel that inlines it (the unit is built
+        // with -fmad=false)
+        const float gmi = rsqrtf(fmaf(uzm, uzm, fmaf(uxm, uxm, 1.f)));
+        const float ty = kH * H * gmi;
+        const float sy = __fdividef(2.f * ty, fmaf(ty, ty, 1.f));
+        const float uxp = fmaf(-uzm, ty, uxm);
+        const float uzp = fmaf(uxm, ty, uzm);
+        uxn = fmaf(kE, E, fmaf(-uzp, sy, uxm));
+        uzn = fmaf(uxp, sy, uzm);
+        const float gi = rsqrtf(fmaf(uzn, uzn, fmaf(uxn, uxn, 1.f)));
+        dz = sc * uzn * gi;
+        jxv = kJ * uxn * gi;
+    }
+    T fm = f + T(0.5) * dz;
+    int cm = c;
+    if (fm >= T(1)) { cm += 1; fm -= T(1); } else if (fm < T(0)) { cm -= 1; fm += T(1); }
+    m.nx0 = cm;
+    m.jx0 = jxv * (T(1) - fm);
+    m.jx1 = jxv * fm;
+    T f1 = f + dz;
+    int c1 = c;
+    if (f1 >= T(1)) { c1 += 1; f1 -= T(1); } else if (f1 < T(0)) { c1 -= 1; f1 += T(1); }
+    if (c1 == c) {
+        m.nzA = c; m.jzA = kJz * (f1 - f);
+        m.nzB = -1; m.jzB = T(0);
+    } else if (c1 == c + 1) {
+        m.nzA = c; m.jzA = kJz * (T(1) - f);
+        m.nzB = c + 1; m.jzB = kJz * f1;
+    } else {
+        m.nzA = c - 1; m.jzA = -kJz * (T(1) - f1);
+        m.nzB = c; m.jzB = -kJz * f;
+    }
+    m.c1 = c1;
+    m.f1 = f1;
+    m.ux = uxn;
+    m.uz = uzn;
+}
+
+// Exact 64-bit add into shared memory from two native 32-bit atomics (little-endian halves):
+// the low half's returned old value gives this addition's carry, so the pair always holds the
+// exact 64-bit sum; the high half is skipped when it gains nothing.
+__device__ __forceinline__ void smem_add_u64(unsigned long long *p, unsigned long long v)
+{
+    unsigned *w = reinterpret_cast<unsigned *>(p);
+    const unsigned lo = (unsigned)v, hi = (unsigned)(v >> 32);
+    const unsigned old = atomicAdd(w, lo);
+    const unsigned hadd = hi + ((old + lo < old) ? 1u : 0u);
+    if (hadd) atomicAdd(w + 1, hadd);
+}
 
 // Sum a uint64 over the lanes of `peers` exactly (wrap-around two's complement arithmetic).
 __device__ __forceinline__ unsigned long long peer_sum_u64(unsigned peers, unsigned long long v)
@@ -94,7 +207,7 @@ __device__ __forceinline__ void deposit_slot(unsigned long long *win, unsigned l
         if (leader && node >= 0 && s != 0ull) {
             const int rel = node - base;
             if (rel >= 0 && rel < PIC_WIN)
-                atomicAdd(win + (size_t)(word0 + w) * PIC_WIN + rel, s);
+                smem_add_u64(win + (size_t)(word0 + w) * PIC_WIN + rel, s);
             else
                 atomicAdd(acc + (size_t)(word0 + w) * nz1 + node, s);
         }
@@ -139,41 +252,19 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
             const T E = (T(1) - f) * a.ex[c] + f * a.ex[c + 1];
             const T H = (T(1) - fh) * (T(0.5) * (a.hy[j] + a.hyp[j])) +
                         fh * (T(0.5) * (a.hy[j + 1] + a.hyp[j + 1]));
-            const T uxm = a.ux[p] + a.kE * E;
-            const T uzm = a.uz[p];
-            const T gm = sqrt(T(1) + uxm * uxm + uzm * uzm);
-            const T ty = a.kH * H / gm;
-            const T sy = T(2) * ty / (T(1) + ty * ty);
-            const T uxp = uxm - uzm * ty;
-            const T uzp = uzm + uxm * ty;
-            const T uxn = (uxm - uzp * sy) + a.kE * E;
-            const T uzn = uzm + uxp * sy;
-            const T g = sqrt(T(1) + uxn * uxn + uzn * uzn);
-            const T dz = a.sc * uzn / g;
-            T fm = f + T(0.5) * dz;
-            int cm = c;
-            if (fm >= T(1)) { cm += 1; fm -= T(1); } else if (fm < T(0)) { cm -= 1; fm += T(1); }
-            const T jxv = a.kJ * uxn / g;
-            nx0 = cm;
-            nx1 = cm + 1;
-            Fix<T>::split(jxv * (T(1) - fm), a.jscale, a.jscale_f, vx0);
-            Fix<T>::split(jxv * fm, a.jscale, a.jscale_f, vx1);
-            T f1 = f + dz;
-            int c1 = c;
-            if (f1 >= T(1)) { c1 += 1; f1 -= T(1); } else if (f1 < T(0)) { c1 -= 1; f1 += T(1); }
-            if (c1 == c) {
-                nzA = c;
-                Fix<T>::split(a.kJz * (f1 - f), a.jscale, a.jscale_f, vzA);
-            } else if (c1 == c + 1) {
-                nzA = c;
-                nzB = c + 1;
-                Fix<T>::split(a.kJz * (T(1) - f), a.jscale, a.jscale_f, vzA);
-                Fix<T>::split(a.kJz * f1, a.jscale, a.jscale_f, vzB);
-            } else {
-                nzA = c - 1;
-                nzB = c;
-                Fix<T>::split(-a.kJz * (T(1) - f1), a.jscale, a.jscale_f, vzA);
-                Fix<T>::split(-a.kJz * f, a.jscale, a.jscale_f, vzB);
+            Moved<T> m;
+            particle_step<T>(E, H, c, f, a.ux[p], a.uz[p], a.kE, a.kH, a.sc, a.kJ, a.kJz, m);
+            const T uxn = m.ux, uzn = m.uz, f1 = m.f1;
+            int c1 = m.c1;
+            nx0 = m.nx0;
+            nx1 = m.nx0 + 1;
+            Fix<T>::split(m.jx0, a.jscale, a.jscale_f, vx0);
+            Fix<T>::split(m.jx1, a.jscale, a.jscale_f, vx1);
+            nzA = m.nzA;
+            nzB = m.nzB;
+            if (a.deposit_jz) {
+                Fix<T>::split(m.jzA, a.jscale, a.jscale_f, vzA);
+                if (nzB >= 0) Fix<T>::split(m.jzB, a.jscale, a.jscale_f, vzB);
             }
             if (c1 >= a.chi) c1 -= Lc;
             else if (c1 < a.clo) c1 += Lc;
@@ -184,8 +275,10 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
         }
         deposit_slot<W>(win, a.acc, nz1, base, 0, nx0, vx0);
         deposit_slot<W>(win, a.acc, nz1, base, 0, nx1, vx1);
-        deposit_slot<W>(win, a.acc, nz1, base, W, nzA, vzA);
-        deposit_slot<W>(win, a.acc, nz1, base, W, nzB, vzB);
+        if (a.deposit_jz) {
+            deposit_slot<W>(win, a.acc, nz1, base, W, nzA, vzA);
+            deposit_slot<W>(win, a.acc, nz1, base, W, nzB, vzB);
+        }
     }
     if (lost) atomicAdd(a.status, lost);
     __syncthreads();
@@ -441,7 +534,7 @@ struct PicPlan {
 // Enqueue one step; `sorted` selects which buffer holds the particles (flips when re-binning).
 template <typename T>
 void pic_enqueue_step(PicPlan<T> &P, const PicBeam &bm, int t, bool do_sort, bool &in_b,
-                      bool device_step, cudaStream_t st, PicTimer *tm)
+                      bool device_step, cudaStream_t st, PicTimer *tm, bool last_step)
 {
     if (do_sort) {
         int32_t *cS = in_b ? P.cellB : P.cellA, *cD = in_b ? P.cellA : P.cellB;
@@ -464,6 +557,7 @@ void pic_enqueue_step(PicPlan<T> &P, const PicBeam &bm, int t, bool do_sort, boo
     P.pa.uz = in_b ? P.uzB : P.uzA;
     if (bm.n_part > 0) {
         if (tm) tm->begin(&tm->out->push_ms);
+        P.pa.deposit_jz = last_step ? 1 : 0;
         pic_push_kernel<T><<<P.pblocks, PIC_THREADS, 0, st>>>(P.pa);
         if (tm) tm->end();
     }
@@ -551,7 +645,8 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
     // one captured block = two re-binning periods, so the particles end where they started
     const int K = sorting ? 2 * bm.sort_every : 64;
     const int total = h.step_end - h.step_begin;
-    const int nblocks = (timing || !allow_graphs) ? 0 : total / K;
+    // graph blocks never cover the last step (it deposits Jz), so at most (total-1)/K blocks
+    const int nblocks = (timing || !allow_graphs || total < 1) ? 0 : (total - 1) / K;
     bool in_b = false;
     int t = h.step_begin;
     if (nblocks > 0) {
@@ -580,7 +675,7 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
             bool cb = false;
             for (int j = 0; j < K; ++j)
                 pic_enqueue_step<T>(P, bm, 0, sorting && (j % bm.sort_every) == 0, cb, true, cs,
-                                    nullptr);
+                                    nullptr, false);
             cudaGraph_t graph = nullptr;
             e = cudaStreamEndCapture(cs, &graph);
             if (e != cudaSuccess) return cuda_status(e);
@@ -598,7 +693,7 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
     }
     for (; t < h.step_end; ++t)
         pic_enqueue_step<T>(P, bm, t, sorting && ((t - h.step_begin) % bm.sort_every) == 0, in_b,
-                            false, st, timing ? &tmr : nullptr);
+                            false, st, timing ? &tmr : nullptr, t == h.step_end - 1);
     if (in_b && bm.n_part > 0) {
         const size_t np = (size_t)bm.n_part;
         e = cudaMemcpyAsync(cell, P.cellB, np * 4, cudaMemcpyDeviceToDevice, st);
@@ -611,6 +706,7 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
     pic_finish_kernel<T><<<P.fblocks, P.threads, 0, st>>>(fa.state + h.state_offset, nz1, status);
     if (timing) {
         timing->steps = total;
+        timing->path = 1;
         cudaEventDestroy(tmr.ev[0]);
         cudaEventDestroy(tmr.ev[1]);
     }

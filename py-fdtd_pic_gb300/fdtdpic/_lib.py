@@ -26,7 +26,7 @@ UNITS = {
     "fdtd1d_f64.cu": ["-fmad=false"],
     "fdtd1d_f32.cu": [],
     "pic_f64.cu": ["-fmad=false"],
-    "pic_f32.cu": [],
+    "pic_f32.cu": ["-fmad=false"],  # PIC paths agree bit for bit (explicit fmaf in the push)
     "dft.cu": [],
     "noalloc.cu": [],
 }
@@ -141,6 +141,8 @@ def _declare(L):
     L.fdtdpic_pic_jscale.argtypes = [P]
     L.fdtdpic_run.restype = c_int
     L.fdtdpic_run.argtypes = [c_int] + [P] * 16 + [c_i64, P, P, P]
+    L.fdtdpic_pic_scratch_bytes.restype = c_i64
+    L.fdtdpic_pic_scratch_bytes.argtypes = [c_int, P, P]
     L.fdtdpic_run_noalloc.restype = c_int
     L.fdtdpic_run_noalloc.argtypes = [c_int] + [P] * 17
     for name, argt in _EXTRA_DECLS.items():

@@ -23,13 +23,14 @@ M_E = 9.1093837139e-31
 
 class FdtdPicTiming(ctypes.Structure):
     _fields_ = [("push_ms", ctypes.c_float), ("field_ms", ctypes.c_float),
-                ("sort_ms", ctypes.c_float), ("steps", ctypes.c_int32)]
+                ("sort_ms", ctypes.c_float), ("steps", ctypes.c_int32),
+                ("path", ctypes.c_int32)]
 
 
 class PicBeam(ctypes.Structure):
     _fields_ = [("n_part", ctypes.c_int32), ("clo", ctypes.c_int32), ("chi", ctypes.c_int32),
                 ("sort_every", ctypes.c_int32), ("chunk", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("kE", ctypes.c_double), ("kH", ctypes.c_double),
+                ("path", ctypes.c_int32), ("kE", ctypes.c_double), ("kH", ctypes.c_double),
                 ("sc", ctypes.c_double), ("kJ", ctypes.c_double), ("kJz", ctypes.c_double),
                 ("jscale", ctypes.c_double)]
 
@@ -73,10 +74,13 @@ def beam_constants(dz, dt, weight, mu0, q=Q_E, m=M_E):
 
 
 class PicRun:
-    """One grid plus a beam, resident on the GPU; ``step(n)`` advances n steps."""
+    """One grid plus a beam, resident on the GPU; ``step(n)`` advances n steps.
+
+    path: "auto" (the persistent tiled kernel when the grid can be tiled over the SMs, else the
+    streaming kernels), "streaming" or "tiled"."""
 
     def __init__(self, grid: Grid, beam: Beam, dz: float, dt: float, mu0: float,
-                 precision="f32", sort_every=32, chunk=0, device=None):
+                 precision="f32", sort_every=32, chunk=0, path="auto", device=None):
         _require_cuda()
         self.L = lib()
         self.prec, self.tdt = _dtype(precision)
@@ -109,7 +113,9 @@ class PicRun:
         for name, v in self.constants.items():
             setattr(self.pb, name, v)
         self.pb.jscale = self.L.fdtdpic_pic_jscale(ctypes.byref(self.pb))
-        self.scratch_bytes = int(self.L.fdtdpic_scratch_bytes(self.prec, g.nz, beam.n))
+        self.pb.path = {"auto": 0, "streaming": 1, "tiled": 2}[path]
+        self.scratch_bytes = int(self.L.fdtdpic_pic_scratch_bytes(
+            self.prec, self.desc.ctypes.data, ctypes.byref(self.pb)))
         self.d_scratch = torch.zeros(max(1, self.scratch_bytes), dtype=torch.uint8, device=dev)
         self.step_done = 0
 

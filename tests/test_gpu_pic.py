@@ -19,14 +19,15 @@ def _torch():
     return torch
 
 
-def _case(precision, sort_every=32, chunk=0, steps=(T,)):
+def _case(precision, sort_every=32, chunk=0, steps=(T,), path="auto"):
     torch = _torch()
     import scipy.constants as sc
     from fdtdpic.grid import lorentz_kerr_grid
     from fdtdpic.pic import PicRun, make_beam
     g = lorentz_kerr_grid(NZ, T, front=300, rear=400, nzsrc=60, probes=(50, 350), chi3=1e-2)
     beam = make_beam(NPART, CLO, CHI, DZ)
-    run = PicRun(g, beam, DZ, DT, sc.mu_0, precision=precision, sort_every=sort_every, chunk=chunk)
+    run = PicRun(g, beam, DZ, DT, sc.mu_0, precision=precision, sort_every=sort_every, chunk=chunk,
+                 path=path)
     snaps = []
     for s in steps:
         run.step(s)
@@ -55,8 +56,9 @@ def _zeta(cell, frac):
     return cell + frac
 
 
-def test_pic_fp64_matches_oracle():
-    g, beam, run, snaps = _case("f64")
+@pytest.mark.parametrize("path", ["streaming", "tiled"])
+def test_pic_fp64_matches_oracle(path):
+    g, beam, run, snaps = _case("f64", path=path)
     f, (cell, frac, ux, uz), (jx, jz) = snaps[-1]
     r, (oc, of, oux, ouz) = _oracle(g, beam)
     assert run.status()[0] == 0 and r["lost"] == 0
@@ -71,8 +73,9 @@ def test_pic_fp64_matches_oracle():
     assert O.rel_l2(uz, ouz) <= 1e-14
 
 
-def test_pic_fp32_error_vs_fp64_oracle():
-    g, beam, run, snaps = _case("f32")
+@pytest.mark.parametrize("path", ["streaming", "tiled"])
+def test_pic_fp32_error_vs_fp64_oracle(path):
+    g, beam, run, snaps = _case("f32", path=path)
     f, (cell, frac, ux, uz), (jx, jz) = snaps[-1]
     r, (oc, of, oux, ouz) = _oracle(g, beam)
     assert run.status()[0] == 0
@@ -85,10 +88,11 @@ def test_pic_fp32_error_vs_fp64_oracle():
     assert O.rel_l2(uz, ouz) <= 1e-6
 
 
-@pytest.mark.parametrize("precision", ["f32", "f64"])
-def test_pic_run_to_run_bit_stable(precision):
-    _, _, run1, s1 = _case(precision, sort_every=16)
-    _, _, run2, s2 = _case(precision, sort_every=16)
+@pytest.mark.parametrize("precision,path", [("f32", "streaming"), ("f64", "streaming"),
+                                            ("f32", "tiled"), ("f64", "tiled")])
+def test_pic_run_to_run_bit_stable(precision, path):
+    _, _, run1, s1 = _case(precision, sort_every=16, path=path)
+    _, _, run2, s2 = _case(precision, sort_every=16, path=path)
     for k in ("Ex", "Hy", "Dx"):
         np.testing.assert_array_equal(s1[-1][0][k], s2[-1][0][k])
     for a, b in zip(s1[-1][1], s2[-1][1]):
@@ -98,23 +102,25 @@ def test_pic_run_to_run_bit_stable(precision):
 
 def test_pic_result_independent_of_binning_and_chunking():
     """Deposits are exact integer sums: re-binning cadence and CTA chunking change nothing."""
-    _, _, _, a = _case("f32", sort_every=0, chunk=512)
-    _, _, _, b = _case("f32", sort_every=7, chunk=2048)
+    _, _, _, a = _case("f32", sort_every=0, chunk=512, path="streaming")
+    _, _, _, b = _case("f32", sort_every=7, chunk=2048, path="streaming")
     np.testing.assert_array_equal(a[-1][0]["Ex"], b[-1][0]["Ex"])
     np.testing.assert_array_equal(a[-1][2][0], b[-1][2][0])
     for x, y in zip(a[-1][1], b[-1][1]):
         np.testing.assert_array_equal(x, y)
 
 
-def test_pic_resume_in_chunks_equals_one_call():
-    _, _, _, whole = _case("f64", steps=(T,))
-    _, _, _, parts = _case("f64", steps=(250, 200, 150))
+@pytest.mark.parametrize("path", ["streaming", "tiled"])
+def test_pic_resume_in_chunks_equals_one_call(path):
+    _, _, _, whole = _case("f64", steps=(T,), path=path)
+    _, _, _, parts = _case("f64", steps=(250, 200, 150), path=path)
     for k in ("Ex", "Hy", "Dx"):
         np.testing.assert_array_equal(whole[-1][0][k], parts[-1][0][k])
 
 
-def test_pic_gpu_jz_conserves_charge():
-    g, beam, run, snaps = _case("f64", steps=(T - 1, 1))
+@pytest.mark.parametrize("path", ["streaming", "tiled"])
+def test_pic_gpu_jz_conserves_charge(path):
+    g, beam, run, snaps = _case("f64", steps=(T - 1, 1), path=path)
     (_, (c0, f0, _, _), _), (_, (c1, f1, _, _), (jx, jz)) = snaps
     qw = O.Q_E * beam.weight
 
@@ -127,3 +133,20 @@ def test_pic_gpu_jz_conserves_charge():
     h = np.arange(CLO + 2, CHI - 2)
     resid = (charge(c1, f1)[h] - charge(c0, f0)[h]) / DT + (jz[h] - jz[h - 1]) / DZ
     assert np.abs(resid).max() <= 1e-9 * np.abs(jz).max() / DZ
+
+
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_tiled_kernel_equals_streaming_kernels_bitwise(precision):
+    """Same arithmetic per cell and per particle, exact integer deposits: identical bits, although
+    one path is a single persistent launch with neighbour handshakes and the other three
+    launches per step."""
+    _, _, r1, a = _case(precision, path="streaming")
+    _, _, r2, b = _case(precision, path="tiled")
+    assert r1.status()[0] == 0 and r2.status()[0] == 0 and r2.status()[1] == 0
+    for k in ("Ex", "Hy", "Dx", "psiE", "psiH", "A"):
+        np.testing.assert_array_equal(a[-1][0][k], b[-1][0][k], err_msg=k)
+    np.testing.assert_array_equal(a[-1][2][0], b[-1][2][0])
+    np.testing.assert_array_equal(a[-1][2][1], b[-1][2][1])
+    np.testing.assert_array_equal(r1.probes(), r2.probes())
+    for x, y in zip(a[-1][1], b[-1][1]):
+        np.testing.assert_array_equal(x, y)
