@@ -21,7 +21,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "../../include/fdtdpic.h"
+#include "fdtdpic.h"
 #include "cubic.cuh"
 
 namespace fdtdpic {

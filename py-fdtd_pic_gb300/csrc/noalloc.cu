@@ -19,7 +19,7 @@
 // event or stream creation.
 #include <cuda_runtime.h>
 
-#include "../../include/fdtdpic.h"
+#include "fdtdpic.h"
 #include "pic_kernel.cuh"
 
 namespace fdtdpic {

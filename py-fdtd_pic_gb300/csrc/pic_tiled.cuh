@@ -303,21 +303,35 @@ __global__ void __launch_bounds__(TILE_THREADS, 1) pic_tiled_kernel(TileArgs<T> 
                 }
                 pid = idU[u];
             }
-            for (int d = -1; d < MIG_DIRS; ++d) {
-                const unsigned mk = __ballot_sync(0xffffffffu, dir == d);
-                if (mk == 0u) continue;
-                const int leader = __ffs(mk) - 1;
+            // stayers: one ballot and one shared atomic per warp; movers (a few per step) take
+            // the general per-direction loop
+            const unsigned stay_mk = __ballot_sync(0xffffffffu, dir == -1);
+            const unsigned move_mk = __ballot_sync(0xffffffffu, dir >= 0);
+            if (stay_mk) {
+                const int leader = __ffs(stay_mk) - 1;
                 int slot0 = 0;
-                if (lane == leader) slot0 = atomicAdd(d < 0 ? &s_nstay : &s_nout[d], __popc(mk));
+                if (lane == leader) slot0 = atomicAdd(&s_nstay, __popc(stay_mk));
                 slot0 = __shfl_sync(0xffffffffu, slot0, leader);
-                if (dir != d) continue;
-                const int o = slot0 + __popc(mk & lt_mask);
-                if (d < 0) {
-                    if (o >= a.cap) { atomicCAS(&s_err, 0, FDTDPIC_ERR_OOM); continue; }
-                    const size_t r = seg + o;
-                    cellN[r] = cn; fracN[r] = m.f1; uxN[r] = m.ux;
-                    uzN[r] = m.uz; idN[r] = pid;
-                } else {
+                if (dir == -1) {
+                    const int o = slot0 + __popc(stay_mk & lt_mask);
+                    if (o < a.cap) {
+                        const size_t r = seg + o;
+                        cellN[r] = cn; fracN[r] = m.f1; uxN[r] = m.ux; uzN[r] = m.uz; idN[r] = pid;
+                    } else {
+                        atomicCAS(&s_err, 0, FDTDPIC_ERR_OOM);
+                    }
+                }
+            }
+            if (move_mk) {
+                for (int d = 0; d < MIG_DIRS; ++d) {
+                    const unsigned mk = __ballot_sync(0xffffffffu, dir == d);
+                    if (mk == 0u) continue;
+                    const int leader = __ffs(mk) - 1;
+                    int slot0 = 0;
+                    if (lane == leader) slot0 = atomicAdd(&s_nout[d], __popc(mk));
+                    slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+                    if (dir != d) continue;
+                    const int o = slot0 + __popc(mk & lt_mask);
                     if (o >= a.mig_cap) { atomicCAS(&s_err, 0, FDTDPIC_ERR_OOM); continue; }
                     const size_t r = (((size_t)par * a.G + b) * MIG_DIRS + d) * a.mig_cap + o;
                     a.mcell[r] = cn; a.mfrac[r] = m.f1; a.mux[r] = m.ux; a.muz[r] = m.uz;
