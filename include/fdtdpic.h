@@ -159,6 +159,28 @@ int fdtd1d_run_global(int precision, const FdtdInstance *h_inst, const FdtdInsta
  * d_coef: n x 4 doubles (a,b,c,d); d_out: n doubles. */
 int fdtdpic_cubic_root0(int n, const double *d_coef, double *d_out, fdtdpic_stream_t stream);
 
+/* ---- reflection vs frequency ---------------------------------------------------------------
+ * The reference turns probe traces into a reflection coefficient with an FFT and a peak-bin
+ * ratio (TransformHandler.RefTester, TransformHandler.py:34-78; MasterController.results,
+ * MasterController.py:485-500).  Here every requested frequency is a direct DFT of every trace,
+ * batched: X[r, f] = sum_n x[r, n] exp(-2 pi i f_k n dt), FP32 products, FP64 accumulation of
+ * 64-step chunks. */
+/* Bytes of the twiddle table for F frequencies and S samples (F x S float2). */
+int64_t fdtdpic_dft_twiddle_bytes(int F, int S);
+/* Fill the twiddle table (phase reduced in FP64, values in FP32); d_freqs: F doubles [Hz]. */
+int fdtdpic_dft_twiddles(const double *d_freqs, int F, int S, double dt, void *d_tw,
+                         fdtdpic_stream_t stream);
+/* X (R x F complex, as interleaved doubles) of R traces of S samples.  Trace r, sample n is
+ * element (r / rp) * ldp + (r % rp) * sp + n * sn of d_traces (FDTDPIC_F32 or FDTDPIC_F64); the
+ * probe buffer of a batch with equal step counts is read in place with rp = 2, ldp = 2 S,
+ * sp = 1, sn = 2. */
+int fdtdpic_dft_probes(int precision, const void *d_traces, int R, int S, int rp, int64_t ldp,
+                       int64_t sp, int64_t sn, const void *d_tw, int F, double *d_out,
+                       fdtdpic_stream_t stream);
+/* |R(f)| = |X[2p+1, f]| / |X[2p, f]| for n_pairs trace pairs (0 where |X[2p, f]| = 0). */
+int fdtdpic_reflection_ratio(const double *d_X, int n_pairs, int F, double *d_ratio,
+                             fdtdpic_stream_t stream);
+
 /* ---- FDTD + electron-beam PIC -------------------------------------------------------------
  * Replaces the reference's Jx hook (MasterController.py:93,159; the -Jx term of ADE_ExUpdate,
  * BaseFDTD11.py:667), which the reference never fills; the beam model has no reference code.

@@ -143,6 +143,15 @@ def _declare(L):
     L.fdtdpic_run.argtypes = [c_int] + [P] * 16 + [c_i64, P, P, P]
     L.fdtdpic_pic_scratch_bytes.restype = c_i64
     L.fdtdpic_pic_scratch_bytes.argtypes = [c_int, P, P]
+    L.fdtdpic_dft_twiddle_bytes.restype = c_i64
+    L.fdtdpic_dft_twiddle_bytes.argtypes = [c_int, c_int]
+    L.fdtdpic_dft_twiddles.restype = c_int
+    L.fdtdpic_dft_twiddles.argtypes = [P, c_int, c_int, ctypes.c_double, P, P]
+    L.fdtdpic_dft_probes.restype = c_int
+    L.fdtdpic_dft_probes.argtypes = [c_int, P, c_int, c_int, c_int, c_i64, c_i64, c_i64, P,
+                                     c_int, P, P]
+    L.fdtdpic_reflection_ratio.restype = c_int
+    L.fdtdpic_reflection_ratio.argtypes = [P, c_int, c_int, P, P]
     L.fdtdpic_run_noalloc.restype = c_int
     L.fdtdpic_run_noalloc.argtypes = [c_int] + [P] * 17
     for name, argt in _EXTRA_DECLS.items():
