@@ -173,8 +173,9 @@ int64_t fdtd1d_resident_smem_bytes(const FdtdInstance *inst, int precision)
     if (check_instance(*inst) != FDTDPIC_OK) return 0;
     const int64_t bytes = (precision == FDTDPIC_F64 ? resident_elems<double>(*inst) * 8
                                                     : resident_elems<float>(*inst) * 4);
-    // 227 KiB is the sm_100-family opt-in maximum per CTA; the launch re-checks the device.
-    return bytes <= 227 * 1024 ? bytes : 0;
+    // 227 KiB is the sm_100-family opt-in maximum per CTA, of which 1 KiB stays for the
+    // kernel's static shared variables; the launch re-checks the device.
+    return bytes <= 226 * 1024 ? bytes : 0;
 }
 
 int fdtd1d_run_batch(int precision, int n_inst, const FdtdInstance *d_inst, const int32_t *d_order,

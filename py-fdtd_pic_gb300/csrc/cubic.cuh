@@ -12,6 +12,13 @@
 //   Cells whose discriminant is within 1e-3 of zero (branch choice uncertain in FP32), whose
 //   Newton residual stays large, or whose values are not finite are re-solved with the FP64
 //   closed form and counted.
+//   Monotone case first: with a >= 0, b >= 0, c > 0 and d < 0 the cubic rises on x > 0 from
+//   p(0) = d < 0, so its largest real root is its only positive root, and it is simple.  The
+//   positive root x_q of b x^2 + c x + d (stable form -2d / (c + sqrt(c^2 - 4bd))) has
+//   p(x_q) = a x_q^3 >= 0, so x_q lies at or above the root, where p is convex; Newton from x_q
+//   then falls monotonically onto the root.  Three steps, then the same residual test; a cell
+//   that fails it takes the closed-form path.  This is the Kerr slab's usual case (a = chi3'^2,
+//   b = 2 Re(alpha3 eps chi3), c = |eps|^2, d = -|Dx/eps0|^2).
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -53,9 +60,10 @@ __host__ __device__ inline double cubic_root0_f64(double a, double b, double c, 
 
 // Per-instance constants of the FP32 path, folded in FP64 from (a, b, c).
 struct KerrF32 {
-    float a, b, c, ia, bo3a, g0, f3, j2, inv2i, a3, b2;
+    float a, b, c, ia, bo3a, g0, f3, j2, inv2i, a3, b2, b4, c2;
     double ad, bd, cd;
     int kind;  // 0: general cubic, 1: linear (a=b=0), 2: quadratic (a=0) -> FP64
+    int mono;  // a >= 0, b >= 0, c > 0: the monotone case applies for every d < 0
 };
 
 __device__ inline KerrF32 kerr_f32_setup(double a, double b, double c)
@@ -64,6 +72,8 @@ __device__ inline KerrF32 kerr_f32_setup(double a, double b, double c)
     k.ad = a; k.bd = b; k.cd = c;
     k.a = (float)a; k.b = (float)b; k.c = (float)c;
     k.a3 = (float)(3.0 * a); k.b2 = (float)(2.0 * b);
+    k.b4 = (float)(4.0 * b); k.c2 = (float)(c * c);
+    k.mono = (a >= 0.0 && b >= 0.0 && c > 0.0 && !(a == 0.0 && b == 0.0)) ? 1 : 0;
     if (a == 0.0) {
         k.kind = (b == 0.0) ? 1 : 2;
         k.ia = k.bo3a = k.g0 = k.f3 = k.j2 = k.inv2i = 0.f;
@@ -91,6 +101,18 @@ __device__ inline KerrF32 kerr_f32_setup(double a, double b, double c)
 __device__ inline float cubic_root0_f32(const KerrF32 &k, float d, int *n_fallback)
 {
     if (k.kind == 1) return -d / k.c;
+    if (k.mono && d < 0.f) {
+        float x = __fdividef(-2.f * d, k.c + sqrtf(fmaf(-k.b4, d, k.c2)));
+#pragma unroll
+        for (int it = 0; it < 3; ++it) {
+            const float p = fmaf(fmaf(fmaf(k.a, x, k.b), x, k.c), x, d);
+            const float dp = fmaf(fmaf(k.a3, x, k.b2), x, k.c);
+            x -= __fdividef(p, dp);
+        }
+        const float p = fmaf(fmaf(fmaf(k.a, x, k.b), x, k.c), x, d);
+        const float mag = fabsf(k.c * x) + fabsf(d) + fabsf(k.b * x * x) + fabsf(k.a * x * x * x);
+        if (isfinite(x) && fabsf(p) <= 1e-5f * mag) return x;
+    }
     bool fb = (k.kind != 0);
     float x = 0.f;
     if (!fb) {

@@ -277,10 +277,19 @@ __device__ void run_instance_resident(const BatchArgs<T> &args, int idx, T *smem
     T *probe = args.probe + I.probe_offset;
     T *hist = args.hist ? args.hist + I.hist_offset : nullptr;
     int nfb = 0;
+    // Source values of step t, (T)(Exs[t]/Sc) and (T)(Hys[t]/Sc): one thread divides (in FP64)
+    // one step ahead into a double buffer that the step-closing barrier publishes.
+    __shared__ T s_src[2][2];
+    __syncthreads();  // a previous instance of this CTA may still read s_src
+    if (tid == 0 && I.step_begin < I.step_end) {
+        s_src[I.step_begin & 1][0] = (T)(Exs[I.step_begin] / I.sc);
+        s_src[I.step_begin & 1][1] = I.tfsf ? (T)(Hys[I.step_begin] / I.sc) : T(0);
+    }
+    __syncthreads();
 
     for (int t = I.step_begin; t < I.step_end; ++t) {
-        const T src_e = (T)(Exs[t] / I.sc);
-        const T src_h = I.tfsf ? (T)(Hys[t] / I.sc) : T(0);
+        const T src_e = s_src[t & 1][0];
+        const T src_h = s_src[t & 1][1];
         T *a_out = (t == I.step_end - 1) ? gA : nullptr;
         for (int k = 1 + tid; k < n; k += nt)
             e_cell<T>(I, c, kr, s, k, src_e, src_h, (const T *)nullptr, a_out, &nfb);
@@ -294,6 +303,10 @@ __device__ void run_instance_resident(const BatchArgs<T> &args, int idx, T *smem
             const int row = t / I.hist_interval;
             if (row < I.hist_rows)
                 for (int k = tid; k < n; k += nt) hist[(int64_t)row * n + k] = s.ex[k];
+        }
+        if (tid == nt - 1 && t + 1 < I.step_end) {
+            s_src[(t + 1) & 1][0] = (T)(Exs[t + 1] / I.sc);
+            s_src[(t + 1) & 1][1] = I.tfsf ? (T)(Hys[t + 1] / I.sc) : T(0);
         }
         __syncthreads();
     }
