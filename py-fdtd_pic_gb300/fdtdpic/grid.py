@@ -96,8 +96,11 @@ def _table_and_coef(P, free_space):
     return ps.pml_table(P, arrays), ue, ue_slab, uh, uh_slab
 
 
-def grids_from_reference(P, V, C_P, integrator: str, Exs=None, Hys=None, hist=True):
+def grids_from_reference(P, V, C_P, integrator: str, Exs=None, Hys=None, hist=True,
+                         probe_finish_be=None, probe_start_af=None):
     """The grid(s) one reference integrator call runs; ``Exs``/``Hys`` override SourceManager.
+    ``probe_finish_be``/``probe_start_af`` are the integrators' probeReadFinishBe /
+    probeReadStartAf arguments (default: Controller's int(0.7 T) and int(0.05 T)).
 
     V.plasmaFreqE is updated as the reference's integrators update it (spatialStab rescale:
     once for the Kerr integrator, once per pass -- compounding -- for the Lorentz one)."""
@@ -112,7 +115,8 @@ def grids_from_reference(P, V, C_P, integrator: str, Exs=None, Hys=None, hist=Tr
     for k in ("kappaMax", "r_scale", "r_a_scale", "sigmaOpt", "alphaMax"):
         setattr(CP, k, getattr(C_P, k))
     n_hist = int(T / P.vidInterval) if hist and P.vidInterval > 0 else 0
-    fin_be, st_af = int(T * 0.7), int(T * 0.05)
+    fin_be = int(T * 0.7) if probe_finish_be is None else int(probe_finish_be)
+    st_af = int(T * 0.05) if probe_start_af is None else int(probe_start_af)
 
     if integrator == "IntegratorNL1D":
         table, ue, ue_s, uh, uh_s = _table_and_coef(CP_with(CP, P), False)

@@ -42,3 +42,29 @@ def sources_of(g):
     if bool(g["source_supplied"]):
         return g["Exs"], g["Hys"]
     return None, None
+
+
+def compat_objects(g):
+    """(V, P, C_V, C_P) of fdtdpic.compat.MasterController built as the fixture's generator
+    built the reference's objects (tests/golden/make_golden.py: make_params + setters)."""
+    from fdtdpic.compat import MasterController as MC
+    C0 = 299792458.0
+    sc = lambda k: g["P_" + k][()].item()  # noqa: E731
+    nz, steps, dz, f = int(sc("Nz")), int(sc("timeSteps")), sc("dz"), sc("freq_in")
+    P = MC.Params(nz, steps, 0, 0, 1.0, 1.0, 1.0, 1.0, int(sc("x1Loc")), int(sc("x2Loc")),
+                  int(sc("materialFrontEdge")), int(sc("materialRearEdge")), int(sc("pmlWidth")),
+                  int(sc("nzsrc")), C0 / f, dz, sc("delT"), sc("courantNo"), 1.0 / f, 10.0, False,
+                  nz * dz, f, 20)
+    P.vidInterval = int(sc("vidInterval"))
+    for k in ("TFSF", "SineCont", "Gaussian", "nonLinMed", "LorentzMed", "CPMLXp", "CPMLXm"):
+        setattr(P, k, bool(sc(k)))
+    P.FreeSpace = not (P.nonLinMed or P.LorentzMed)
+    P.Periods, P.Amplitude = sc("Periods"), sc("Amplitude")
+    P.epsRe, P.muRe = sc("epsRe"), sc("muRe")
+    V = MC.Variables(P.Nz, P.timeSteps, P.vidInterval, 1)
+    V.plasmaFreqE, V.gammaE = float(g["plasmaFreqE_in"]), float(g["gammaE"])
+    V.omega_0E, V.chi3Stat = float(g["omega_0E"]), float(g["chi3Stat"])
+    C_P = MC.CPML_Params(P.dz)
+    C_P.kappaMax, C_P.alphaMax = float(g["kappaMax"]), float(g["alphaMax"])
+    C_V = MC.CPML_Variables(P.Nz, P.timeSteps)
+    return V, P, C_V, C_P
