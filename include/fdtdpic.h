@@ -257,6 +257,62 @@ int fdtdpic_run_noalloc(int precision, const FdtdInstance *h_inst, const FdtdIns
                         void *d_uz, int32_t *d_id, void *d_jx, void *d_jz, void *d_hyp,
                         int32_t *d_status, fdtdpic_stream_t stream);
 
+/* ---- served requests: continuous batching over slots ---------------------------------------
+ * No counterpart in the reference, which runs one simulation per script invocation
+ * (MasterController.LoopedSim, MasterController.py:530-600, loops over runs one at a time).
+ * A slot is one admitted request with its own device buffers; a work item is a chunk of its
+ * steps.  fdtdpic_slots_run runs a list of work items in one launch: each CTA takes the next
+ * item from d_queue and steps that request's chunk alone, its fields in shared memory when they
+ * fit (otherwise in the slot's global buffers), its beam (if any) pushed by the same CTA with
+ * exact fixed-point deposits.  A request's results therefore depend only on its own inputs and
+ * its chunk boundaries, never on which other requests share the launch.  Between launches the
+ * caller admits new requests into free slots and retires finished ones. */
+typedef struct FdtdSlot {
+    FdtdInstance inst;     /* offsets are into this slot's buffers below; step_begin, step_end
+                              and resume are taken from the work item */
+    const double *pml_tab; /* FDTD_TAB_ROWS x (2 pml + 1) */
+    const double *src;     /* Exs[n_steps] then Hys[n_steps] */
+    void *state;           /* FDTD_STATE_ARRAYS x (nz+1), precision's type */
+    void *probe;           /* [n_steps][2] */
+    void *hist;            /* [hist_rows][nz+1] or NULL */
+    int32_t n_part;        /* 0: a field-only request; the beam fields below are then unused */
+    int32_t clo, chi;      /* periodic beam domain [clo, chi), 2 <= clo < chi <= nz-2 */
+    int32_t reserved;
+    int32_t *cell;         /* n_part particles: cell, frac, ux, uz as for fdtdpic_run */
+    void *frac, *ux, *uz;
+    void *hyp;             /* (nz+1): Hy one half step back */
+    void *jx, *jz;         /* (nz+1): the last step's grid currents */
+    uint64_t *acc;         /* 2 x words x (nz+1) deposit accumulators (words: 1 for FDTDPIC_F32,
+                              2 for FDTDPIC_F64), used when they do not fit shared memory */
+    double kE, kH, sc, kJ, kJz, jscale; /* as PicBeam */
+    int32_t status[4];     /* written by the kernel: [0] += particles outside the grid,
+                              [1] |= FDTD_STATUS_* bits, [2] += FP64 cubic re-solves */
+} FdtdSlot;
+
+typedef struct FdtdSlotItem {
+    int32_t slot;  /* index into the slot array */
+    int32_t t0;    /* steps [t0, t1) of that request */
+    int32_t t1;
+    int32_t first; /* 1: t0 starts the request (zero fields, zero beam history) */
+} FdtdSlotItem;
+
+/* Like fdtdpic_instance_layout, for FdtdSlot. */
+int fdtdpic_slot_layout(int64_t *out, int n);
+/* Host-side check of one slot descriptor before it is admitted (FDTDPIC_OK or ERR_ARG). */
+int fdtdpic_slot_check(int precision, const FdtdSlot *slot);
+/* Shared memory (bytes) with which this slot's fields (field-only request) or deposit
+ * accumulators (beam request) stay on chip; host-only. */
+int64_t fdtdpic_slot_smem_bytes(int precision, const FdtdSlot *slot);
+/* Run n_items work items over n_slots slots (both arrays in device memory) in one launch.
+ * d_queue: one int32 of caller scratch, reset by this call.  smem_bytes: dynamic shared memory
+ * per CTA (items whose slot needs more run from global memory).  threads_per_cta <= 0 picks
+ * 512; grid_ctas <= 0 the occupancy-limited grid.  Items naming a slot outside [0, n_slots) or
+ * a step range outside [0, n_steps] are skipped and flagged in the slot's status[1]
+ * (FDTD_STATUS_SKIPPED) when the slot exists. */
+int fdtdpic_slots_run(int precision, FdtdSlot *d_slots, int n_slots, const FdtdSlotItem *d_items,
+                      int n_items, int32_t *d_queue, int64_t smem_bytes, int threads_per_cta,
+                      int grid_ctas, fdtdpic_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

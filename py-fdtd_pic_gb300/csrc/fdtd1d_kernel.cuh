@@ -215,11 +215,12 @@ __host__ __device__ inline int64_t resident_elems(const FdtdInstance &I)
     return 2 * n + nslab * (S > 0 ? S : 0) + 2 * W + FDTD_TAB_ROWS * W;
 }
 
-// One instance, all requested steps, fields resident in shared memory.
+// One instance, all requested steps, fields resident in shared memory.  I is the instance's
+// descriptor (offsets into the args' buffers); idx indexes the status/fallback words.
 template <typename T>
-__device__ void run_instance_resident(const BatchArgs<T> &args, int idx, T *smem)
+__device__ void run_instance_resident(const BatchArgs<T> &args, const FdtdInstance &I, int idx,
+                                      T *smem)
 {
-    const FdtdInstance I = args.inst[idx];
     const int tid = threadIdx.x, nt = blockDim.x;
     const int n = I.nz + 1;
     const int W = 2 * I.pml + 1;
@@ -348,7 +349,7 @@ __global__ void __launch_bounds__(1024) fdtd_batch_kernel(BatchArgs<T> args)
             if (threadIdx.x == 0 && args.status) atomicOr(args.status + idx, FDTD_STATUS_SKIPPED);
             continue;
         }
-        run_instance_resident<T>(args, idx, smem);
+        run_instance_resident<T>(args, args.inst[idx], idx, smem);
         __syncthreads();
     }
 }

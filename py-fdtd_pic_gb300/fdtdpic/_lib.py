@@ -28,6 +28,7 @@ UNITS = {
     "pic_f64.cu": ["-fmad=false"],
     "pic_f32.cu": ["-fmad=false"],  # PIC paths agree bit for bit (explicit fmaf in the push)
     "dft.cu": [],
+    "slot.cu": ["-fmad=false"],  # beam requests round as fdtdpic_run's step
     "noalloc.cu": [],
 }
 
@@ -152,6 +153,14 @@ def _declare(L):
                                      c_int, P, P]
     L.fdtdpic_reflection_ratio.restype = c_int
     L.fdtdpic_reflection_ratio.argtypes = [P, c_int, c_int, P, P]
+    L.fdtdpic_slot_layout.restype = c_int
+    L.fdtdpic_slot_layout.argtypes = [P, c_int]
+    L.fdtdpic_slot_check.restype = c_int
+    L.fdtdpic_slot_check.argtypes = [c_int, P]
+    L.fdtdpic_slot_smem_bytes.restype = c_i64
+    L.fdtdpic_slot_smem_bytes.argtypes = [c_int, P]
+    L.fdtdpic_slots_run.restype = c_int
+    L.fdtdpic_slots_run.argtypes = [c_int, P, c_int, P, c_int, P, c_i64, c_int, c_int, P]
     L.fdtdpic_run_noalloc.restype = c_int
     L.fdtdpic_run_noalloc.argtypes = [c_int] + [P] * 17
     for name, argt in _EXTRA_DECLS.items():

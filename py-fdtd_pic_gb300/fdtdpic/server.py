@@ -1,0 +1,489 @@
+"""Serving sweep requests with continuous batching.
+
+A request is one grid run (any size, any step count) with an optional electron beam.  The
+server keeps every admitted request's fields and particles resident in HBM and advances all of
+them together in *rounds*: one launch of ``fdtdpic_slots_run`` whose work items are chunks of
+the active requests' steps, one CTA per item (include/fdtdpic.h).  Between rounds it admits
+waiting requests into free slots as HBM budget allows and retires the ones whose last chunk
+ran.  Chunk lengths come from a per-step cost model so that every item takes about the same
+time; a short request therefore finishes in a few rounds while long ones keep running beside
+it, and a request that arrives mid-run joins at the next round.  Rounds are enqueued ahead of
+the GPU (at most ``max_inflight`` at a time); the host only waits for a round to read back the
+probes of the requests that finished in it.
+
+Results do not depend on the mix: a request's arithmetic is fixed by its own inputs and chunk
+boundaries, and beam deposits are exact integer sums.
+
+No counterpart in the reference, which runs one simulation per ``Controller`` call
+(MasterController.py:451-469) and sweeps by looping over them (``LoopedSim``, :530-600).
+"""
+from __future__ import annotations
+
+import collections
+import ctypes
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import physics_setup as ps
+from ._lib import F32, F64, INSTANCE_DTYPE, STATE_ARRAYS, check, lib
+from .engine import _dtype, _require_cuda
+from .grid import Grid, lorentz_kerr_grid, pack
+from .pic import C0, Beam, PicBeam, beam_constants
+
+_PTR = "<u8"
+SLOT_DTYPE = np.dtype([
+    ("inst", INSTANCE_DTYPE), ("pml_tab", _PTR), ("src", _PTR), ("state", _PTR),
+    ("probe", _PTR), ("hist", _PTR), ("n_part", "<i4"), ("clo", "<i4"), ("chi", "<i4"),
+    ("reserved", "<i4"), ("cell", _PTR), ("frac", _PTR), ("ux", _PTR), ("uz", _PTR),
+    ("hyp", _PTR), ("jx", _PTR), ("jz", _PTR), ("acc", _PTR), ("kE", "<f8"), ("kH", "<f8"),
+    ("sc", "<f8"), ("kJ", "<f8"), ("kJz", "<f8"), ("jscale", "<f8"), ("status", "<i4", (4,)),
+], align=True)
+ITEM_DTYPE = np.dtype([("slot", "<i4"), ("t0", "<i4"), ("t1", "<i4"), ("first", "<i4")])
+
+
+def check_slot_layout(L=None):
+    L = L or lib()
+    n = L.fdtdpic_slot_layout(None, 0)
+    out = np.zeros(n, np.int64)
+    L.fdtdpic_slot_layout(out.ctypes.data, n)
+    names = ["inst", "pml_tab", "src", "state", "probe", "hist", "n_part", "clo", "chi",
+             "reserved", "cell", "frac", "ux", "uz", "hyp", "jx", "jz", "acc", "kE", "kH", "sc",
+             "kJ", "kJz", "jscale", "status"]
+    want = [SLOT_DTYPE.itemsize] + [SLOT_DTYPE.fields[f][1] for f in names] + [ITEM_DTYPE.itemsize]
+    if list(out) != want:
+        raise RuntimeError(f"FdtdSlot layout mismatch: C {list(out)} vs numpy {want}")
+
+
+@dataclass
+class Request:
+    """One run to serve: a grid, an optional beam (with its physical constants), an arrival
+    time on the server's clock.  ``grid_fn``/``beam_fn`` build the grid/beam when the request
+    is admitted (a stream of many requests then costs nothing until they run); ``nz``,
+    ``n_steps``, ``n_part`` describe them before that."""
+    grid: Grid | None = None
+    beam: Beam | None = None
+    dz: float = 0.015
+    dt: float = 0.0
+    mu0: float = 4e-7 * math.pi
+    arrival: float = 0.0
+    rid: int = -1
+    grid_fn: object = None
+    beam_fn: object = None
+    nz: int = 0
+    n_steps: int = 0
+    n_part: int = 0
+    pml: int = 20
+
+    def __post_init__(self):
+        if self.grid is not None:
+            self.nz, self.n_steps, self.pml = self.grid.nz, self.grid.n_steps, self.grid.pml
+        if self.beam is not None:
+            self.n_part = self.beam.n
+
+
+@dataclass
+class Done:
+    rid: int
+    arrival: float
+    admitted: float
+    finished: float
+    probes: np.ndarray
+    status: np.ndarray
+    fields: dict | None = None
+    particles: dict | None = None
+
+    @property
+    def latency(self):
+        return self.finished - self.arrival
+
+
+@dataclass
+class _Active:
+    req: Request
+    slot: int
+    bufs: dict
+    nbytes: int
+    next_step: int
+    cost_ns: float  # predicted ns per step for one CTA
+    admitted: float
+    outs: dict = field(default_factory=dict)
+
+
+class Server:
+    """Continuous-batching server on one GPU.
+
+    precision: "f32" (default) or "f64"; hbm_budget: bytes of request buffers held at once;
+    max_active: requests resident at once (default 2 x the CTAs one round runs); chunk_ms: the
+    target duration of one work item; keep_state: also return final fields and particles."""
+
+    def __init__(self, precision="f32", hbm_budget=150e9, max_active=None, chunk_ms=3.0,
+                 threads=512, smem_bytes=64 * 1024, max_inflight=2, keep_state=False,
+                 device=None, clock=time.perf_counter):
+        _require_cuda()
+        self.L = lib()
+        check_slot_layout(self.L)
+        self.prec, self.tdt = _dtype(precision)
+        self.W = 2 if self.prec == F64 else 1
+        self.dev = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+        self.budget = float(hbm_budget)
+        self.threads = threads
+        self.smem = int(smem_bytes)
+        props = torch.cuda.get_device_properties(self.dev)
+        per_sm = max(1, min(2048 // threads, (228 * 1024) // (self.smem + 1024)))
+        self.ctas = per_sm * props.multi_processor_count
+        self.max_active = int(max_active or 2 * self.ctas)
+        self.chunk_ns = chunk_ms * 1e6
+        self.max_inflight = max_inflight
+        self.keep_state = keep_state
+        self.clock = clock
+        self.stream = torch.cuda.Stream(device=self.dev)
+        n = self.max_active
+        self.h_slots = torch.zeros(n * SLOT_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+        self.slots_np = self.h_slots.numpy().view(SLOT_DTYPE)
+        self.d_slots = torch.zeros(n * SLOT_DTYPE.itemsize, dtype=torch.uint8, device=self.dev)
+        self.d_queue = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self.free = list(range(n - 1, -1, -1))
+        self.active: dict[int, _Active] = {}
+        self.pending: collections.deque = collections.deque()
+        self.bytes_in_use = 0
+        self.inflight: collections.deque = collections.deque()
+        self.done: list[Done] = []
+        # cost model: ns per step per CTA = a_cell * (nz+1) * (1 or global factor) + a_part * np
+        self.a_cell, self.a_cell_global, self.a_part = 2.5, 6.0, 4.0
+        self.scale = 1.0
+        self.rounds = 0
+        self.cell_steps = 0.0
+        self.particle_steps = 0.0
+        self.gpu_ms = 0.0
+        self._items_pin = [torch.zeros(n * ITEM_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+                           for _ in range(max_inflight + 1)]
+        self._items_dev = [torch.zeros(n * ITEM_DTYPE.itemsize, dtype=torch.uint8,
+                                       device=self.dev) for _ in range(max_inflight + 1)]
+        self._ring = 0
+
+    # ---- sizes and costs --------------------------------------------------------------------
+    def request_bytes(self, req: Request) -> int:
+        ts = 8 if self.prec == F64 else 4
+        n = req.nz + 1
+        b = (STATE_ARRAYS * n * ts + 2 * req.n_steps * ts + 2 * req.n_steps * 8 +
+             8 * (2 * req.pml + 1) * 8)
+        if req.n_part:
+            b += req.n_part * (4 + 3 * ts) + 3 * n * ts + 2 * self.W * n * 8
+        return int(b) + 4096
+
+    def _step_cost_ns(self, g: Grid, n_part: int) -> float:
+        resident = n_part == 0 and self._resident_bytes(g) <= self.smem
+        a = self.a_cell if resident else self.a_cell_global
+        slab = max(0, g.rear - g.front)
+        return self.scale * (a * (g.nz + 1 + 4 * slab) + self.a_part * n_part) + 200.0
+
+    def _resident_bytes(self, g: Grid) -> int:
+        d = g.descriptor()
+        return int(self.L.fdtd1d_resident_smem_bytes(np.ascontiguousarray(d).ctypes.data,
+                                                      self.prec) or (1 << 40))
+
+    # ---- admission ----------------------------------------------------------------------------
+    def submit(self, req: Request):
+        self.pending.append(req)
+
+    def _admit(self, now):
+        admitted = 0
+        while self.pending and self.free:
+            req = self.pending[0]
+            need = self.request_bytes(req)
+            if self.bytes_in_use + need > self.budget and self.active:
+                break
+            self.pending.popleft()
+            self._place(req, need, now)
+            admitted += 1
+        return admitted
+
+    def _place(self, req: Request, need: int, now: float):
+        if req.grid is None:
+            req.grid = req.grid_fn()
+        if req.beam is None and req.beam_fn is not None:
+            req.beam = req.beam_fn()
+        g = req.grid
+        ts, tdt, dev = (8 if self.prec == F64 else 4), self.tdt, self.dev
+        n = g.nz + 1
+        slot = self.free.pop()
+        with torch.cuda.stream(self.stream):
+            pk = pack([g], ts)
+            desc = pk["desc"][0].copy()
+            desc["step_begin"], desc["step_end"], desc["resume"] = 0, g.n_steps, 0
+            bufs = dict(
+                table=torch.from_numpy(pk["table"]).pin_memory().to(dev, non_blocking=True),
+                src=torch.from_numpy(pk["src"]).pin_memory().to(dev, non_blocking=True),
+                state=torch.empty(pk["n_state"], dtype=tdt, device=dev),
+                probe=torch.zeros(pk["n_probe"], dtype=tdt, device=dev))
+            s = self.slots_np[slot:slot + 1]  # a view: assignments land in the pinned table
+            s[...] = np.zeros(1, SLOT_DTYPE)
+            s["inst"] = desc
+            s["pml_tab"], s["src"] = bufs["table"].data_ptr(), bufs["src"].data_ptr()
+            s["state"], s["probe"] = bufs["state"].data_ptr(), bufs["probe"].data_ptr()
+            n_part = 0
+            if req.beam is not None and req.beam.n > 0:
+                b = req.beam
+                n_part = b.n
+
+                def up(a, dt_):
+                    return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().to(
+                        dev, dtype=dt_, non_blocking=True)
+                bufs.update(cell=up(b.cell.astype(np.int32), torch.int32), frac=up(b.frac, tdt),
+                            ux=up(b.ux, tdt), uz=up(b.uz, tdt),
+                            hyp=torch.empty(n, dtype=tdt, device=dev),
+                            jx=torch.empty(n, dtype=tdt, device=dev),
+                            jz=torch.empty(n, dtype=tdt, device=dev),
+                            acc=torch.empty(2 * self.W * n, dtype=torch.int64, device=dev))
+                pb = PicBeam()
+                pb.n_part, pb.clo, pb.chi = b.n, b.clo, b.chi
+                consts = beam_constants(req.dz, req.dt, b.weight, req.mu0)
+                for k, v in consts.items():
+                    setattr(pb, k, v)
+                jscale = self.L.fdtdpic_pic_jscale(ctypes.byref(pb))
+                s["n_part"], s["clo"], s["chi"] = b.n, b.clo, b.chi
+                for k in ("cell", "frac", "ux", "uz", "hyp", "jx", "jz", "acc"):
+                    s[k] = bufs[k].data_ptr()
+                for k, v in consts.items():
+                    s[k] = v
+                s["jscale"] = jscale
+            rc = self.L.fdtdpic_slot_check(self.prec, s.ctypes.data)
+            if rc != 0:
+                self.free.append(slot)
+                raise ValueError(f"request {req.rid} rejected by fdtdpic_slot_check ({rc})")
+            sz = SLOT_DTYPE.itemsize
+            self.d_slots[slot * sz:(slot + 1) * sz].copy_(
+                self.h_slots[slot * sz:(slot + 1) * sz], non_blocking=True)
+        self.bytes_in_use += need
+        self.active[slot] = _Active(req=req, slot=slot, bufs=bufs, nbytes=need, next_step=0,
+                                    cost_ns=self._step_cost_ns(g, n_part), admitted=now)
+
+    # ---- rounds ---------------------------------------------------------------------------------
+    def _round(self, now):
+        if not self.active:
+            return False
+        items = []
+        finishing = []
+        pred_ns = 0.0
+        work = [0.0, 0.0]  # cell-steps, particle-steps of this round
+        for slot, a in self.active.items():
+            g = a.req.grid
+            if a.next_step >= g.n_steps:
+                continue
+            k = max(1, int(self.chunk_ns / max(a.cost_ns, 1.0)))
+            t0 = a.next_step
+            t1 = min(g.n_steps, t0 + k)
+            items.append((slot, t0, t1, 1 if t0 == 0 else 0))
+            pred_ns += a.cost_ns * (t1 - t0)
+            work[0] += (g.nz + 1) * (t1 - t0)
+            work[1] += a.req.n_part * (t1 - t0)
+            a.next_step = t1
+            if t1 >= g.n_steps:
+                finishing.append(a)
+        if not items:
+            return False
+        # longest items first: the queue then ends with short ones
+        items.sort(key=lambda it: -self.active[it[0]].cost_ns * (it[2] - it[1]))
+        r = self._ring
+        self._ring = (self._ring + 1) % len(self._items_pin)
+        arr = self._items_pin[r].numpy().view(ITEM_DTYPE)
+        for i, (slot, t0, t1, first) in enumerate(items):
+            arr[i] = (slot, t0, t1, first)
+        nb = len(items) * ITEM_DTYPE.itemsize
+        with torch.cuda.stream(self.stream):
+            self._items_dev[r][:nb].copy_(self._items_pin[r][:nb], non_blocking=True)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(self.stream)
+            check(self.L.fdtdpic_slots_run(
+                self.prec, ctypes.c_void_p(self.d_slots.data_ptr()), self.max_active,
+                ctypes.c_void_p(self._items_dev[r].data_ptr()), len(items),
+                ctypes.c_void_p(self.d_queue.data_ptr()), self.smem, self.threads, 0,
+                ctypes.c_void_p(self.stream.cuda_stream)), "fdtdpic_slots_run")
+            e1.record(self.stream)
+            for a in finishing:
+                a.outs["probe"] = a.bufs["probe"].to("cpu", non_blocking=True)
+                sz = SLOT_DTYPE.itemsize
+                a.outs["slot"] = self.d_slots[a.slot * sz:(a.slot + 1) * sz].to(
+                    "cpu", non_blocking=True)
+                if self.keep_state:
+                    a.outs["state"] = a.bufs["state"].to("cpu", non_blocking=True)
+                    for k in ("cell", "frac", "ux", "uz", "jx", "jz"):
+                        if k in a.bufs:
+                            a.outs[k] = a.bufs[k].to("cpu", non_blocking=True)
+            done_ev = torch.cuda.Event()
+            done_ev.record(self.stream)
+        for a in finishing:
+            del self.active[a.slot]
+        self.inflight.append((done_ev, e0, e1, finishing, pred_ns, len(items), work))
+        self.rounds += 1
+        return True
+
+    def _complete(self, block=False):
+        n = 0
+        while self.inflight:
+            ev, e0, e1, finishing, pred_ns, n_items, work = self.inflight[0]
+            if not block and not ev.query():
+                break
+            ev.synchronize()
+            self.inflight.popleft()
+            now = self.clock()
+            ms = e0.elapsed_time(e1)
+            self.gpu_ms += ms
+            self.cell_steps += work[0]
+            self.particle_steps += work[1]
+            # calibrate the cost model: a round lasts about its predicted work over the CTAs
+            if pred_ns > 0 and n_items >= self.ctas // 2:
+                ratio = (ms * 1e6) / (pred_ns / min(self.ctas, n_items))
+                self.scale = min(100.0, max(0.01, 0.8 * self.scale + 0.2 * self.scale * ratio))
+            for a in finishing:
+                g = a.req.grid
+                slot_rec = a.outs["slot"].numpy().view(SLOT_DTYPE)[0]
+                fields = None
+                parts = None
+                if self.keep_state:
+                    st = a.outs["state"].double().numpy()
+                    nn = g.nz + 1
+                    fields = dict(Ex=st[:nn].copy(), Hy=st[nn:2 * nn].copy())
+                    if "jx" in a.outs:
+                        fields.update(Jx=a.outs["jx"].double().numpy(),
+                                      Jz=a.outs["jz"].double().numpy())
+                    if "cell" in a.outs:
+                        parts = {k: a.outs[k].numpy() for k in ("cell", "frac", "ux", "uz")}
+                self.done.append(Done(
+                    rid=a.req.rid, arrival=a.req.arrival, admitted=a.admitted, finished=now,
+                    probes=a.outs["probe"].double().numpy().reshape(g.n_steps, 2),
+                    status=np.array(slot_rec["status"]), fields=fields, particles=parts))
+                self.bytes_in_use -= a.nbytes
+                self.free.append(a.slot)
+                a.bufs.clear()
+                n += 1
+        return n
+
+    # ---- driving --------------------------------------------------------------------------------
+    def poll(self, now=None, block=False):
+        """One scheduling pass: retire finished rounds, admit, enqueue a round if there is
+        room in flight.  Returns the number of requests completed in this pass."""
+        now = self.clock() if now is None else now
+        n = self._complete(block=False)
+        self._admit(now)
+        while len(self.inflight) >= self.max_inflight:
+            n += self._complete(block=True)
+            self._admit(self.clock())
+        self._round(self.clock())
+        if block:
+            n += self._complete(block=True)
+        return n
+
+    def drain(self):
+        """Run until every submitted request has completed."""
+        while self.pending or self.active or self.inflight:
+            self.poll()
+            if not self.active and not self.pending:
+                self._complete(block=True)
+        return self.done
+
+    def run_stream(self, requests, duration):
+        """Real-time run: each request is submitted when the clock reaches its arrival time
+        (seconds from start); stops admitting at ``duration`` and returns the statistics of
+        the requests completed by then."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        t_start = self.clock()
+        i = 0
+        while True:
+            now = self.clock() - t_start
+            while i < len(reqs) and reqs[i].arrival <= now:
+                r = reqs[i]
+                r.arrival = t_start + r.arrival
+                self.submit(r)
+                i += 1
+            if now >= duration:
+                break
+            if not self.active and not self.pending and not self.inflight:
+                if i >= len(reqs):
+                    break
+                time.sleep(min(1e-3, max(0.0, reqs[i].arrival - now)))
+                continue
+            self.poll()
+        elapsed = self.clock() - t_start
+        self._complete(block=False)
+        return self.stats(elapsed, submitted=i)
+
+    def stats(self, elapsed, submitted=None):
+        lat = np.array([d.latency for d in self.done])
+        svc = np.array([d.finished - d.admitted for d in self.done])
+        pct = (lambda a, q: float(np.percentile(a, q)) if a.size else None)
+        return dict(completed=len(self.done), submitted=submitted, elapsed_s=elapsed,
+                    throughput_rps=len(self.done) / elapsed if elapsed > 0 else 0.0,
+                    p50_s=pct(lat, 50), p99_s=pct(lat, 99), service_p50_s=pct(svc, 50),
+                    service_p99_s=pct(svc, 99), queue_depth=len(self.pending),
+                    active=len(self.active), rounds=self.rounds,
+                    mcell_steps_per_s=self.cell_steps / elapsed / 1e6 if elapsed > 0 else 0.0,
+                    mparticle_steps_per_s=self.particle_steps / elapsed / 1e6
+                    if elapsed > 0 else 0.0, gpu_busy_s=self.gpu_ms / 1e3)
+
+
+# ------------------------------------------------------------------------------------------
+# the served request stream: Poisson arrivals, ragged grids, optional beams
+# ------------------------------------------------------------------------------------------
+def make_request_stream(rate=2000.0, duration=60.0, seed=20261203, nz_lo=256, nz_hi=65536,
+                        steps_lo=1000, steps_hi=50000, np_max=2_000_000, dz=0.015, sc=0.5,
+                        max_requests=None):
+    """Seeded stream: arrivals Poisson(rate) over [0, duration); per request
+    Nz = round(exp U[ln nz_lo, ln nz_hi]), steps ~ U{steps_lo..steps_hi},
+    Np = floor(exp U[0, ln(np_max + 1)]) - 1 (0 included), material as the batched sweep
+    (slab width U[0.05, 0.30] Nz centred between the source and the far PML, d_eps U[0.5, 4],
+    f0 U[0.8, 2.5] GHz, chi3 logU[1e-4, 1e-1]), Kerr integrator, Gaussian-modulated 1 GHz
+    source at cell 100, probes at 50 and Nz-50; beam over cells [50, Nz-51), vz ~ N(0.3c,
+    0.003c), density 1e14 m^-3.  Beams are generated when a request is admitted."""
+    from .pic import make_beam
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t, arrivals = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            break
+        arrivals.append(t)
+        if max_requests and len(arrivals) >= max_requests:
+            break
+    n = len(arrivals)
+    nz = np.rint(np.exp(rng.uniform(np.log(nz_lo), np.log(nz_hi), n))).astype(int)
+    steps = rng.integers(steps_lo, steps_hi + 1, n)
+    npart = (np.floor(np.exp(rng.uniform(0.0, np.log(np_max + 1.0), n))) - 1).astype(int)
+    width = rng.uniform(0.05, 0.30, n)
+    deps = rng.uniform(0.5, 4.0, n)
+    f0 = rng.uniform(0.8e9, 2.5e9, n)
+    chi3 = 10.0 ** rng.uniform(-4, -1, n)
+    seeds = rng.integers(0, 2 ** 62, n)
+    dt = sc * dz / C0
+    src_cache = {}
+
+    def grid_of(N, T, front, rear, d_eps, f, chi):
+        if T not in src_cache:
+            src_cache[T] = ps.gauss_sine(T, 1e9, dt)
+        return lorentz_kerr_grid(N, T, dz=dz, sc=sc, front=front, rear=rear, pml=20, nzsrc=100,
+                                 probes=(50, N - 50), d_eps=d_eps, f0=f, chi3=chi,
+                                 source=src_cache[T])
+
+    reqs = []
+    for i in range(n):
+        N, T = int(nz[i]), int(steps[i])
+        pml, nzsrc = 20, 100
+        w = max(1, int(round(width[i] * N)))
+        centre = (nzsrc + (N - pml)) // 2
+        front = max(nzsrc + 2, centre - w // 2)
+        rear = max(front, min(N - pml - 2, front + w))
+        r = Request(dz=dz, dt=dt, arrival=arrivals[i], rid=i, nz=N, n_steps=T, pml=pml,
+                    grid_fn=(lambda N=N, T=T, fr=front, re=rear, de=float(deps[i]),
+                             f=float(f0[i]), ch=float(chi3[i]): grid_of(N, T, fr, re, de, f, ch)))
+        if npart[i] > 0:
+            clo, chi, npi, sd = 50, N - 51, int(npart[i]), int(seeds[i])
+            r.beam_fn = (lambda npi=npi, clo=clo, chi=chi, sd=sd:
+                         make_beam(npi, clo, chi, dz, seed=sd))
+            r.n_part = npi
+        reqs.append(r)
+    return reqs
