@@ -252,12 +252,125 @@ def run_ours(args):
         "gpu_launches": launches_per_run * args.steps,
         "clocks": clk.summary(),
     }
+    for name, fn in (("sweep", bench_sweep), ("serve", bench_serve), ("large", bench_large)):
+        if name in args.extra:
+            try:
+                out[name] = fn(args, flush)
+            except Exception as e:  # a failing extra section must not hide the headline line
+                out[name] = {"error": f"{type(e).__name__}: {e}"}
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
     return out
+
+
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def bench_sweep(args, flush):
+    """The 4096-instance batched sweep (Nz ~ U{500..8000}, 8192 steps, Kerr slabs of random
+    width and material, FP32): one persistent launch for all instances, then the 4096 x 2 probe
+    DFTs at 512 frequencies and |R(f)|.  Compared with the plain form: the same kernel with one
+    instance per launch, launched one after another (timed on the first 16 instances)."""
+    import torch
+    from fdtdpic import sweep
+    spec = sweep.SweepSpec()
+    grids, dt = sweep.make_sweep_grids(spec)
+    sw = sweep.Sweep(grids, dt, spec.freqs(), precision="f32", threads=256)
+    st = torch.cuda.current_stream()
+    sw.run()
+    torch.cuda.synchronize()
+    f_ms, s_ms = [], []
+    for _ in range(max(1, min(args.steps, 3))):
+        flush.fill_(1)
+        a0, a1 = _events()
+        b1 = torch.cuda.Event(enable_timing=True)
+        a0.record()
+        sw.launch_fields(st)
+        a1.record()
+        sw.launch_spectra(st)
+        b1.record()
+        b1.synchronize()
+        f_ms.append(a0.elapsed_time(a1))
+        s_ms.append(a1.elapsed_time(b1))
+    fields_ms, spectra_ms = statistics.median(f_ms), statistics.median(s_ms)
+    cells = sw.cell_steps()
+    status = sw.packed.d_status.cpu().numpy()
+    fallbacks = int(sw.packed.d_fallbacks.cpu().numpy().sum())
+    plain_rate, plain_ms = sweep.plain_per_instance_rate(grids, max_instances=16)
+    batched = cells / ((fields_ms + spectra_ms) * 1e-3)
+    dft_flops = 8.0 * 2 * sw.n * sw.S * sw.F
+    return {"workload": "sweep_4096inst_nz500-8000_steps8192_kerr_f32",
+            "instances": sw.n, "time_steps": sw.S, "freqs": sw.F,
+            "fields_ms": round(fields_ms, 2), "spectra_ms": round(spectra_ms, 2),
+            "mcell_steps_per_s": round(batched / 1e6, 1),
+            "plain_mcell_steps_per_s": round(plain_rate / 1e6, 1),
+            "vs_plain": round(batched / plain_rate, 1),
+            "dft_tflops": round(dft_flops / (spectra_ms * 1e-3) / 1e12, 2),
+            "fp64_cubic_resolves": fallbacks, "bad_status": int((status != 0).sum()),
+            "plain": "same resident kernel, one instance per launch, 16 instances in sequence"}
+
+
+def bench_serve(args, flush):
+    """Continuous-batching server on the served request stream (Poisson arrivals at 2000/s,
+    Nz log-uniform 256-65536, steps 1k-50k, beams of 0-2M particles, sweep materials, FP32,
+    150 GB HBM budget), run in real time for --serve-seconds.  The offered load is far above
+    one GPU's capacity: the numbers are the completed requests' throughput and latency and the
+    queue left at the end."""
+    from fdtdpic import server
+    secs = args.serve_seconds
+    reqs = server.make_request_stream(rate=2000.0, duration=secs)
+    srv = server.Server(precision="f32", hbm_budget=150e9)
+    st = srv.run_stream(reqs, secs)
+    st.update(workload="serve_poisson2000_nz256-65536_steps1k-50k_np0-2M_f32",
+              offered=len(reqs), offered_rps=round(len(reqs) / secs, 1))
+    return {k: (round(v, 3) if isinstance(v, float) else v) for k, v in st.items()}
+
+
+def bench_large(args, flush):
+    """One large instance: Nz = 2^24 cells, 64M macroparticles over the whole grid, Kerr slab
+    over the middle half, FP32, streaming PIC path; timed over --large-steps of its 20,000 steps
+    after a 64-step warm-up (the rate per step is the same over the run)."""
+    import scipy.constants as sc
+    import torch
+    from fdtdpic.grid import lorentz_kerr_grid
+    from fdtdpic.pic import FdtdPicTiming, PicRun, make_beam
+    nz, npart, total = 1 << 24, 64 << 20, 20000
+    g = lorentz_kerr_grid(nz, total, front=nz // 4, rear=3 * nz // 4, nzsrc=NZSRC,
+                          probes=(50, nz - 50), chi3=1e-2)
+    beam = make_beam(npart, 50, nz - 51, DZ, seed=7, sort=False)
+    dt = 0.5 * DZ / 299792458.0
+    run = PicRun(g, beam, DZ, dt, sc.mu_0, precision="f32", sort_every=32)
+    del beam
+    run.step(64)
+    torch.cuda.synchronize()
+    n = args.large_steps
+    e0, e1 = _events()
+    e0.record()
+    run.step(n)
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    tm = FdtdPicTiming()
+    run.step(64, timing=tm)
+    slab = nz // 2
+    alg = (nz * BYTES_PER_CELL + slab * 8 + nz * 8 + npart * BYTES_PER_PARTICLE)
+    peak, kind = _peaks()
+    gbs = alg * n / (ms * 1e-3) / 1e9
+    return {"workload": "large_nz16777216_np67108864_kerr_f32", "timed_steps": n,
+            "ms_per_step": round(ms / n, 3),
+            "mcell_steps_per_s": round(nz * n / (ms * 1e-3) / 1e6, 1),
+            "mparticle_steps_per_s": round(npart * n / (ms * 1e-3) / 1e6, 1),
+            "algorithmic_gbs": round(gbs, 1), "hbm_frac": round(gbs / peak, 3),
+            "peak_source": kind, "bytes_per_step": alg,
+            "kernel_ms_per_step": {"push": round(tm.push_ms / 64, 3),
+                                   "field": round(tm.field_ms / 64, 3),
+                                   "sort": round(tm.sort_ms / 64, 3)},
+            "status": [int(x) for x in run.status()]}
 
 
 def _oracle_setup(n_part):
@@ -347,10 +460,15 @@ def main():
     ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--extra", default="sweep,serve,large",
+                    help="comma-separated extra sections: sweep, serve, large ('' for none)")
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--large-steps", type=int, default=256)
     ap.add_argument("--time-steps", type=int, default=None,
                     help="shorter runs for profiling under ncu (the line is then not a bench "
                          "number and says so in config.time_steps)")
     args = ap.parse_args()
+    args.extra = [x for x in args.extra.split(",") if x]
     if args.time_steps:
         global T
         T = int(args.time_steps)

@@ -43,15 +43,21 @@ int run_pic_tiled_f32(const FdtdInstance &h, const BatchArgs<float> &fa, const P
                       int32_t *id, float *jx, float *jz, float *hyp, unsigned char *scratch,
                       int32_t *status, FdtdPicTiming *timing, cudaStream_t st);
 
-// Tiling of a beam run on the current device, or ok=false when the tiled path does not apply.
-static TileGeom tiled_geometry(const FdtdInstance &h, const PicBeam &b)
+// Tiling of a beam run on the current device, or ok=false when the tiled path does not apply
+// (fewer than two tiles of the minimum width, or a tile's fields beyond shared memory).
+static TileGeom tiled_geometry(int precision, const FdtdInstance &h, const PicBeam &b)
 {
     TileGeom g{};
-    int dev = 0, sms = 0;
+    int dev = 0, sms = 0, max_optin = 0;
     if (b.path == 1 || cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+            cudaSuccess)
         return g;
-    return tile_geometry(h, b, sms);
+    g = tile_geometry(h, b, sms);
+    // 1 KiB stays for the kernel's static shared variables
+    if (g.ok && tile_smem_bytes(precision, g.wmax) > (int64_t)max_optin - 1024) g.ok = false;
+    return g;
 }
 
 // ---- captured PIC step blocks (replayed by calls with identical arguments) -------------
@@ -253,7 +259,7 @@ int64_t fdtdpic_pic_scratch_bytes(int precision, const FdtdInstance *inst, const
     if (!inst || !beam || (precision != FDTDPIC_F64 && precision != FDTDPIC_F32)) return 0;
     if (check_instance(*inst) != FDTDPIC_OK) return 0;
     int64_t need = fdtdpic_scratch_bytes(precision, inst->nz, beam->n_part);
-    const TileGeom tg = tiled_geometry(*inst, *beam);
+    const TileGeom tg = tiled_geometry(precision, *inst, *beam);
     if (tg.ok) {
         const int64_t t = (int64_t)tile_scratch_layout(precision, tg).total;
         if (beam->path == 2 || t > need) need = (beam->path == 2) ? t : (t > need ? t : need);
@@ -283,7 +289,7 @@ int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d
     if (b.path < 0 || b.path > 2) return FDTDPIC_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     unsigned char *scr = (unsigned char *)d_scratch;
-    const TileGeom tg = tiled_geometry(*h_inst, b);
+    const TileGeom tg = tiled_geometry(precision, *h_inst, b);
     const int64_t tiled_need = tg.ok ? (int64_t)tile_scratch_layout(precision, tg).total : -1;
     if (tg.ok && scratch_bytes >= tiled_need) {
         if (precision == FDTDPIC_F64) {

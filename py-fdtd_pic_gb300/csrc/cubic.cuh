@@ -98,6 +98,13 @@ __device__ inline KerrF32 kerr_f32_setup(double a, double b, double c)
     return k;
 }
 
+// The FP64 re-solve, out of line: it is rare, and inlined it would hold registers in every
+// kernel that steps Kerr cells.
+static __device__ __noinline__ float cubic_root0_f64_to_f32(double a, double b, double c, double d)
+{
+    return (float)cubic_root0_f64(a, b, c, d);
+}
+
 __device__ inline float cubic_root0_f32(const KerrF32 &k, float d, int *n_fallback)
 {
     if (k.kind == 1) return -d / k.c;
@@ -144,7 +151,7 @@ __device__ inline float cubic_root0_f32(const KerrF32 &k, float d, int *n_fallba
     }
     if (fb) {
         if (n_fallback) ++*n_fallback;
-        x = (float)cubic_root0_f64(k.ad, k.bd, k.cd, (double)d);
+        x = cubic_root0_f64_to_f32(k.ad, k.bd, k.cd, (double)d);
     }
     return x;
 }

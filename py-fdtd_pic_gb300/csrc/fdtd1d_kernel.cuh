@@ -76,6 +76,45 @@ struct Kerr<float> {
     }
 };
 
+// Per-launch set-up done once per CTA instead of once per thread: the Kerr constants (folded in
+// FP64, whose pipe is narrow) and the step's source values.  Every thread of the CTA must call
+// these (they hold a barrier).
+template <typename T>
+__device__ inline void kerr_setup_block(Kerr<T> &kr, const FdtdInstance &I)
+{
+    __shared__ Kerr<T> s_kr;
+    __syncthreads();  // an earlier use of s_kr by this CTA is finished
+    if (threadIdx.x == 0) s_kr.setup(I);
+    __syncthreads();
+    kr = s_kr;
+}
+
+// make_scal's FP64 -> T conversions also run on the FP64 pipe: once per CTA.
+template <typename T>
+__device__ inline Scal<T> scal_block(const FdtdInstance &I)
+{
+    __shared__ Scal<T> s_c;
+    __syncthreads();
+    if (threadIdx.x == 0) s_c = make_scal<T>(I);
+    __syncthreads();
+    return s_c;
+}
+
+template <typename T>
+__device__ inline void source_block(const FdtdInstance &I, const double *src, int t, T &src_e,
+                                    T &src_h)
+{
+    __shared__ T s_v[2];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s_v[0] = (T)(src[t] / I.sc);
+        s_v[1] = I.tfsf ? (T)(src[I.n_steps + t] / I.sc) : T(0);
+    }
+    __syncthreads();
+    src_e = s_v[0];
+    src_h = s_v[1];
+}
+
 // ---------------------------------------------------------------------------------------
 // storage back ends: shared-memory resident (compact) and global (full-length arrays)
 // ---------------------------------------------------------------------------------------
@@ -109,12 +148,12 @@ struct GlobalStore {
 };
 
 // E phase for cell k in [1, nz].  src_e = Exs[t]/Sc, src_h = Hys[t]/Sc in T.
-// jx (nullable): the beam's grid current, entering the Ex update as the reference's -Jx term
-// and, with the beam on, the slab's Dx update too (dx_jx).
+// has_jx/jxv: the beam's grid current at cell k, entering the Ex update as the reference's -Jx
+// term and, with the beam on, the slab's Dx update too (dx_jx).
 template <typename T, class S>
 __device__ __forceinline__ void e_cell(const FdtdInstance &I, const Scal<T> &c, const Kerr<T> &kr,
-                                       S &s, int k, T src_e, T src_h, const T *jx, T *a_out,
-                                       int *nfb, bool dx_jx = false)
+                                       S &s, int k, T src_e, T src_h, bool has_jx, T jxv,
+                                       T *a_out, int *nfb, bool dx_jx = false)
 {
     const int n = I.nz + 1;
     const T hk = s.Hy(k), hkm = s.Hy(k - 1);
@@ -130,7 +169,7 @@ __device__ __forceinline__ void e_cell(const FdtdInstance &I, const Scal<T> &c, 
     const T den = (col >= 0) ? s.tab_at(FDTD_TAB_DENE, col) : T(1);
     const T up = (I.mode == FDTD_MODE_FREESPACE && slab) ? c.ue_slab : c.ue;
     T dh = hk - hkm;
-    if (jx) dh = dh - jx[k];
+    if (has_jx) dh = dh - jxv;
     ex = ex + dh * up * den;
     if ((I.cpml_lo && k < I.pml) || (I.cpml_hi && k >= n - I.pml)) {
         T &psi = s.PsiE(col, k);
@@ -145,7 +184,7 @@ __device__ __forceinline__ void e_cell(const FdtdInstance &I, const Scal<T> &c, 
             if (k == I.nzsrc) hkm_d = hkm - src_h;
         }
         T dhd = hk_d - hkm_d;
-        if (dx_jx && jx) dhd = dhd - jx[k];
+        if (dx_jx && has_jx) dhd = dhd - jxv;
         const T dx = s.Dx(k) + dhd * c.dtdz * den;
         s.Dx(k) = dx;
         if (I.mode == FDTD_MODE_KERR) {
@@ -293,7 +332,7 @@ __device__ void run_instance_resident(const BatchArgs<T> &args, const FdtdInstan
         const T src_h = s_src[t & 1][1];
         T *a_out = (t == I.step_end - 1) ? gA : nullptr;
         for (int k = 1 + tid; k < n; k += nt)
-            e_cell<T>(I, c, kr, s, k, src_e, src_h, (const T *)nullptr, a_out, &nfb);
+            e_cell<T>(I, c, kr, s, k, src_e, src_h, false, T(0), a_out, &nfb);
         __syncthreads();
         for (int k = 1 + tid; k < n - 1; k += nt) h_cell<T>(I, c, s, k, src_h);
         if (tid == 0) tfsf_edge<T>(I, s, src_h);
@@ -376,31 +415,29 @@ __device__ inline GlobalStore<T> global_store(const FdtdInstance &I, const Batch
 }
 
 template <typename T>
-__global__ void fdtd_global_e_kernel(BatchArgs<T> args, int t)
+__global__ void __launch_bounds__(256, 4) fdtd_global_e_kernel(BatchArgs<T> args, int t)
 {
-    const FdtdInstance &I = args.inst[0];
+    const FdtdInstance I = args.inst[0];  // by value: fields stay in registers
     GlobalStore<T> s = global_store<T>(I, args);
-    const Scal<T> c = make_scal<T>(I);
+    const Scal<T> c = scal_block<T>(I);
     Kerr<T> kr;
-    kr.setup(I);
-    const double *Exs = args.src + I.src_offset;
-    const double *Hys = Exs + I.n_steps;
-    const T src_e = (T)(Exs[t] / I.sc);
-    const T src_h = I.tfsf ? (T)(Hys[t] / I.sc) : T(0);
+    kerr_setup_block<T>(kr, I);
+    T src_e, src_h;
+    source_block<T>(I, args.src + I.src_offset, t, src_e, src_h);
     const int n = I.nz + 1;
     T *gA = args.state + I.state_offset + (int64_t)FDTD_ST_A * n;
     int nfb = 0;
     for (int k = 1 + blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-        e_cell<T>(I, c, kr, s, k, src_e, src_h, (const T *)nullptr, gA, &nfb);
+        e_cell<T>(I, c, kr, s, k, src_e, src_h, false, T(0), gA, &nfb);
     if (nfb && args.fallbacks) atomicAdd(args.fallbacks, nfb);
 }
 
 template <typename T>
-__global__ void fdtd_global_h_kernel(BatchArgs<T> args, int t)
+__global__ void __launch_bounds__(256, 4) fdtd_global_h_kernel(BatchArgs<T> args, int t)
 {
-    const FdtdInstance &I = args.inst[0];
+    const FdtdInstance I = args.inst[0];  // by value: fields stay in registers
     GlobalStore<T> s = global_store<T>(I, args);
-    const Scal<T> c = make_scal<T>(I);
+    const Scal<T> c = scal_block<T>(I);
     const double *Hys = args.src + I.src_offset + I.n_steps;
     const T src_h = I.tfsf ? (T)(Hys[t] / I.sc) : T(0);
     const int n = I.nz + 1;
@@ -413,7 +450,7 @@ __global__ void fdtd_global_h_kernel(BatchArgs<T> args, int t)
 template <typename T>
 __global__ void fdtd_global_probe_kernel(BatchArgs<T> args, int t)
 {
-    const FdtdInstance &I = args.inst[0];
+    const FdtdInstance I = args.inst[0];  // by value: fields stay in registers
     const int n = I.nz + 1;
     const T *ex = args.state + I.state_offset + (int64_t)FDTD_ST_EX * n;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -430,7 +467,7 @@ __global__ void fdtd_global_probe_kernel(BatchArgs<T> args, int t)
 template <typename T>
 __global__ void fdtd_global_init_kernel(BatchArgs<T> args)
 {
-    const FdtdInstance &I = args.inst[0];
+    const FdtdInstance I = args.inst[0];  // by value: fields stay in registers
     const int64_t n = (int64_t)I.nz + 1;
     T *gst = args.state + I.state_offset;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < FDTD_STATE_ARRAYS * n;
@@ -441,7 +478,7 @@ __global__ void fdtd_global_init_kernel(BatchArgs<T> args)
 template <typename T>
 __global__ void fdtd_global_finish_kernel(BatchArgs<T> args)
 {
-    const FdtdInstance &I = args.inst[0];
+    const FdtdInstance I = args.inst[0];  // by value: fields stay in registers
     const int n = I.nz + 1;
     const T *gst = args.state + I.state_offset;
     bool bad = false;

@@ -8,7 +8,7 @@
 //   pic_h_kernel    : H phase, probes, snapshots
 // and every sort_every steps a counting re-bin of the particles by cell (histogram, scan,
 // scatter), which keeps each CTA's particles within a few cells so its deposits land in a small
-// shared-memory window and warp lanes share nodes (warp-segmented sums via __match_any_sync).
+// shared-memory window (exact 64-bit adds from pairs of 32-bit shared atomics).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -180,37 +180,24 @@ __device__ __forceinline__ void smem_add_u64(unsigned long long *p, unsigned lon
     if (hadd) atomicAdd(w + 1, hadd);
 }
 
-// Sum a uint64 over the lanes of `peers` exactly (wrap-around two's complement arithmetic).
-__device__ __forceinline__ unsigned long long peer_sum_u64(unsigned peers, unsigned long long v)
-{
-    const unsigned c0 = (unsigned)(v & 0x3FFFFFull);
-    const unsigned c1 = (unsigned)((v >> 22) & 0x3FFFFFull);
-    const unsigned c2 = (unsigned)(v >> 44);
-    const unsigned long long s0 = __reduce_add_sync(peers, c0);
-    const unsigned long long s1 = __reduce_add_sync(peers, c1);
-    const unsigned long long s2 = __reduce_add_sync(peers, c2);
-    return s0 + (s1 << 22) + (s2 << 44);
-}
-
-// One deposit slot for the whole warp (every lane calls it; invalid lanes pass node = -1).
+// One lane's deposit words: into the CTA's shared window when the node falls in it, else
+// straight into the global accumulators.  (A warp-aggregated form -- match-any plus segmented
+// reductions per node -- measured 3x slower on GB300 than these direct shared atomics.)
 template <int W>
 __device__ __forceinline__ void deposit_slot(unsigned long long *win, unsigned long long *acc,
                                              int nz1, int base, int word0, int node,
                                              const long long *val)
 {
-    const unsigned peers = __match_any_sync(0xffffffffu, node);
-    const int lane = threadIdx.x & 31;
-    const bool leader = (lane == __ffs(peers) - 1);
+    if (node < 0) return;
+    const int rel = node - base;
 #pragma unroll
     for (int w = 0; w < W; ++w) {
-        const unsigned long long s = peer_sum_u64(peers, (unsigned long long)val[w]);
-        if (leader && node >= 0 && s != 0ull) {
-            const int rel = node - base;
-            if (rel >= 0 && rel < PIC_WIN)
-                smem_add_u64(win + (size_t)(word0 + w) * PIC_WIN + rel, s);
-            else
-                atomicAdd(acc + (size_t)(word0 + w) * nz1 + node, s);
-        }
+        const unsigned long long s = (unsigned long long)val[w];
+        if (s == 0ull) continue;
+        if (rel >= 0 && rel < PIC_WIN)
+            smem_add_u64(win + (size_t)(word0 + w) * PIC_WIN + rel, s);
+        else
+            atomicAdd(acc + (size_t)(word0 + w) * nz1 + node, s);
     }
 }
 
@@ -323,9 +310,10 @@ __device__ __forceinline__ void pic_e_cell(PicField<T> &a, const FdtdInstance &I
         a.acc[(size_t)w * n + k] = 0ull;
         a.acc[(size_t)(W + w) * n + k] = 0ull;
     }
-    a.jx[k] = Fix<T>::join(wx, a.jinv, a.jinv_f);
+    const T jxk = Fix<T>::join(wx, a.jinv, a.jinv_f);
+    a.jx[k] = jxk;
     a.jz[k] = Fix<T>::join(wz, a.jinv, a.jinv_f);
-    if (k >= 1) e_cell<T>(I, c, kr, s, k, src_e, src_h, a.jx, gA, nfb, true);
+    if (k >= 1) e_cell<T>(I, c, kr, s, k, src_e, src_h, true, jxk, gA, nfb, true);
 }
 
 template <typename T>
@@ -343,17 +331,16 @@ __device__ __forceinline__ void pic_probes(PicField<T> &a, const FdtdInstance &I
 }
 
 template <typename T>
-__global__ void pic_e_kernel(PicField<T> a, int t_arg)
+__global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
 {
-    const FdtdInstance &I = a.f.inst[0];
+    const FdtdInstance I = a.f.inst[0];  // by value: fields stay in registers
     const int t = pic_step_index(a, t_arg);
     GlobalStore<T> s = global_store<T>(I, a.f);
-    const Scal<T> c = make_scal<T>(I);
+    const Scal<T> c = scal_block<T>(I);
     Kerr<T> kr;
-    kr.setup(I);
-    const double *Exs = a.f.src + I.src_offset;
-    const T src_e = (T)(Exs[t] / I.sc);
-    const T src_h = I.tfsf ? (T)(Exs[I.n_steps + t] / I.sc) : T(0);
+    kerr_setup_block<T>(kr, I);
+    T src_e, src_h;
+    source_block<T>(I, a.f.src + I.src_offset, t, src_e, src_h);
     const int n = I.nz + 1;
     T *gA = a.f.state + I.state_offset + (int64_t)FDTD_ST_A * n;
     int nfb = 0;
@@ -363,12 +350,12 @@ __global__ void pic_e_kernel(PicField<T> a, int t_arg)
 }
 
 template <typename T>
-__global__ void pic_h_kernel(PicField<T> a, int t_arg)
+__global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
 {
-    const FdtdInstance &I = a.f.inst[0];
+    const FdtdInstance I = a.f.inst[0];  // by value: fields stay in registers
     const int t = pic_step_index(a, t_arg);
     GlobalStore<T> s = global_store<T>(I, a.f);
-    const Scal<T> c = make_scal<T>(I);
+    const Scal<T> c = scal_block<T>(I);
     const T src_h = I.tfsf ? (T)(a.f.src[I.src_offset + I.n_steps + t] / I.sc) : T(0);
     const int n = I.nz + 1;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -388,15 +375,14 @@ template <typename T>
 __global__ void __launch_bounds__(1024) pic_field_fused_kernel(PicField<T> a, int32_t *step_w,
                                                                 int t_arg)
 {
-    const FdtdInstance &I = a.f.inst[0];
+    const FdtdInstance I = a.f.inst[0];  // by value: fields stay in registers
     const int t = pic_step_index(a, t_arg);
     GlobalStore<T> s = global_store<T>(I, a.f);
-    const Scal<T> c = make_scal<T>(I);
+    const Scal<T> c = scal_block<T>(I);
     Kerr<T> kr;
-    kr.setup(I);
-    const double *Exs = a.f.src + I.src_offset;
-    const T src_e = (T)(Exs[t] / I.sc);
-    const T src_h = I.tfsf ? (T)(Exs[I.n_steps + t] / I.sc) : T(0);
+    kerr_setup_block<T>(kr, I);
+    T src_e, src_h;
+    source_block<T>(I, a.f.src + I.src_offset, t, src_e, src_h);
     const int n = I.nz + 1;
     T *gA = a.f.state + I.state_offset + (int64_t)FDTD_ST_A * n;
     int nfb = 0;
@@ -420,27 +406,89 @@ static __global__ void pic_hist_kernel(int n_part, const int32_t *cell, int32_t 
     }
 }
 
-// Exclusive scan of counts[0..n) into cursor (one CTA of 1024 threads, contiguous segments).
-static __global__ void __launch_bounds__(1024) pic_scan_kernel(const int32_t *counts, int32_t *cursor, int n)
+// Exclusive scan of counts[0..n) into cursor, three launches over tiles of SCAN_TILE counts:
+// per-tile sums, a scan of the tile sums (one CTA), then each tile's scan plus its offset.
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_PER_THREAD = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_PER_THREAD;
+
+inline int scan_tiles(int n) { return (n + SCAN_TILE - 1) / SCAN_TILE; }
+
+// Block-wide exclusive scan of one int per thread (SCAN_THREADS threads); returns the total.
+__device__ __forceinline__ int block_exclusive_scan(int v, int &excl)
 {
-    __shared__ int part[1024];
-    const int tid = threadIdx.x;
-    const int seg = (n + blockDim.x - 1) / blockDim.x;
-    const int lo = min(n, tid * seg), hi = min(n, lo + seg);
-    int s = 0;
-    for (int i = lo; i < hi; ++i) s += counts[i];
-    part[tid] = s;
-    __syncthreads();
-    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
-        const int v = (tid >= off) ? part[tid - off] : 0;
-        __syncthreads();
-        part[tid] += v;
-        __syncthreads();
+    __shared__ int warp_tot[SCAN_THREADS / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
-    int run = part[tid] - s;
-    for (int i = lo; i < hi; ++i) {
-        cursor[i] = run;
-        run += counts[i];
+    if (lane == 31) warp_tot[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int w = warp_tot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        warp_tot[lane] = w;  // inclusive
+    }
+    __syncthreads();
+    const int before = wid ? warp_tot[wid - 1] : 0;
+    excl = before + x - v;
+    const int total = warp_tot[SCAN_THREADS / 32 - 1];
+    __syncthreads();  // warp_tot may be reused by the next call
+    return total;
+}
+
+static __global__ void __launch_bounds__(SCAN_THREADS) pic_scan_sums_kernel(const int32_t *counts,
+                                                                             int32_t *tile_sum, int n)
+{
+    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+    int s = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_PER_THREAD; ++j)
+        if (base + j < n) s += counts[base + j];
+    int excl;
+    const int tot = block_exclusive_scan(s, excl);
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = tot;
+}
+
+static __global__ void __launch_bounds__(SCAN_THREADS) pic_scan_top_kernel(int32_t *tile_sum, int nt)
+{
+    int carry = 0;
+    for (int b0 = 0; b0 < nt; b0 += SCAN_THREADS) {
+        const int i = b0 + threadIdx.x;
+        const int v = (i < nt) ? tile_sum[i] : 0;
+        int excl;
+        const int tot = block_exclusive_scan(v, excl);
+        if (i < nt) tile_sum[i] = carry + excl;
+        carry += tot;
+    }
+}
+
+static __global__ void __launch_bounds__(SCAN_THREADS) pic_scan_final_kernel(const int32_t *counts,
+                                                                              const int32_t *tile_off,
+                                                                              int32_t *cursor, int n)
+{
+    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+    int c[SCAN_PER_THREAD];
+    int s = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_PER_THREAD; ++j) {
+        c[j] = (base + j < n) ? counts[base + j] : 0;
+        s += c[j];
+    }
+    int run;
+    block_exclusive_scan(s, run);
+    run += tile_off[blockIdx.x];
+#pragma unroll
+    for (int j = 0; j < SCAN_PER_THREAD; ++j) {
+        if (base + j < n) cursor[base + j] = run;
+        run += c[j];
     }
 }
 
@@ -474,7 +522,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Scratch layout shared by the size query and the launcher.
 struct PicScratch {
-    size_t acc, counts, cursor, step, cell2, frac2, ux2, uz2, id2, total;
+    size_t acc, counts, cursor, step, tile_sum, cell2, frac2, ux2, uz2, id2, total;
 };
 inline PicScratch pic_scratch_layout(int tsize, int nz, int n_part)
 {
@@ -486,6 +534,7 @@ inline PicScratch pic_scratch_layout(int tsize, int nz, int n_part)
     L.counts = o; o = align256(o + (nz1 + 1) * 4);
     L.cursor = o; o = align256(o + (nz1 + 1) * 4);
     L.step = o; o = align256(o + 4);
+    L.tile_sum = o; o = align256(o + ((nz1 + SCAN_TILE - 1) / SCAN_TILE + 1) * 4);
     L.cell2 = o; o = align256(o + (size_t)n_part * 4);
     L.frac2 = o; o = align256(o + (size_t)n_part * tsize);
     L.ux2 = o; o = align256(o + (size_t)n_part * tsize);
@@ -525,7 +574,7 @@ struct PicPlan {
     bool fused;
     PicArgs<T> pa;
     PicField<T> pf;
-    int32_t *counts, *cursor, *step;
+    int32_t *counts, *cursor, *step, *tile_sum;
     // particle buffers: A = caller's, B = scratch
     int32_t *cellA, *cellB, *idA, *idB;
     T *fracA, *fracB, *uxA, *uxB, *uzA, *uzB;
@@ -545,7 +594,11 @@ void pic_enqueue_step(PicPlan<T> &P, const PicBeam &bm, int t, bool do_sort, boo
         if (tm) tm->begin(&tm->out->sort_ms);
         cudaMemsetAsync(P.counts, 0, (size_t)(P.nz1 + 1) * 4, st);
         pic_hist_kernel<<<P.sblocks, P.threads, 0, st>>>(bm.n_part, cS, P.counts, P.nz1);
-        pic_scan_kernel<<<1, 1024, 0, st>>>(P.counts, P.cursor, P.nz1);
+        const int ntile = scan_tiles(P.nz1);
+        pic_scan_sums_kernel<<<ntile, SCAN_THREADS, 0, st>>>(P.counts, P.tile_sum, P.nz1);
+        pic_scan_top_kernel<<<1, SCAN_THREADS, 0, st>>>(P.tile_sum, ntile);
+        pic_scan_final_kernel<<<ntile, SCAN_THREADS, 0, st>>>(P.counts, P.tile_sum, P.cursor,
+                                                               P.nz1);
         pic_scatter_kernel<T><<<P.sblocks, P.threads, 0, st>>>(bm.n_part, cS, fS, xS, zS, iS,
                                                               P.cursor, P.nz1, cD, fD, xD, zD, iD);
         if (tm) tm->end();
@@ -601,6 +654,7 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
     P.counts = (int32_t *)(scratch + L.counts);
     P.cursor = (int32_t *)(scratch + L.cursor);
     P.step = (int32_t *)(scratch + L.step);
+    P.tile_sum = (int32_t *)(scratch + L.tile_sum);
     P.cellA = cell; P.fracA = frac; P.uxA = ux; P.uzA = uz; P.idA = id;
     P.cellB = (int32_t *)(scratch + L.cell2);
     P.fracB = (T *)(scratch + L.frac2);

@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 1) pic_tiled_kernel(TileArgs<T> 
         __syncthreads();
         const T src_e = s_src[0], src_h = s_src[1];
         for (int k = max(c0, 1) + tid; k < c1; k += nt)
-            e_cell<T>(I, sc, kr, s, k, src_e, src_h, jloc - base, gA, &nfb, true);
+            e_cell<T>(I, sc, kr, s, k, src_e, src_h, true, jloc[k - base], gA, &nfb, true);
         __syncthreads();
         // ---------------- round B: boundary Ex ----------------
         if (tid == 0) {

@@ -67,7 +67,7 @@ __device__ void run_instance_cta_global(const BatchArgs<T> &args, const FdtdInst
         const T src_h = s_src[t & 1][1];
         T *a_out = (t == I.step_end - 1) ? gA : nullptr;
         for (int k = 1 + tid; k < n; k += nt)
-            e_cell<T>(I, c, kr, s, k, src_e, src_h, (const T *)nullptr, a_out, &nfb);
+            e_cell<T>(I, c, kr, s, k, src_e, src_h, false, T(0), a_out, &nfb);
         __syncthreads();
         for (int k = 1 + tid; k < n - 1; k += nt) h_cell<T>(I, c, s, k, src_h);
         if (tid == 0) tfsf_edge<T>(I, s, src_h);
@@ -201,9 +201,10 @@ __device__ void run_beam_slot(FdtdSlot &S, const FdtdInstance &I, unsigned char 
                 acc[(size_t)w * n + k] = 0ull;
                 acc[(size_t)(W + w) * n + k] = 0ull;
             }
-            jx[k] = Fix<T>::join(wx, jinv, jinv_f);
+            const T jxk = Fix<T>::join(wx, jinv, jinv_f);
+            jx[k] = jxk;
             jz[k] = Fix<T>::join(wz, jinv, jinv_f);
-            if (k >= 1) e_cell<T>(I, c, kr, s, k, src_e, src_h, jx, gA, &nfb, true);
+            if (k >= 1) e_cell<T>(I, c, kr, s, k, src_e, src_h, true, jxk, gA, &nfb, true);
         }
         __syncthreads();
         for (int k = 1 + tid; k < n - 1; k += nt) h_cell<T>(I, c, s, k, src_h);

@@ -52,15 +52,17 @@ class Beam:
         return len(self.cell)
 
 
-def make_beam(n_part, clo, chi, dz, density=1e14, v_mean=0.3, v_spread=0.003, seed=20261203):
+def make_beam(n_part, clo, chi, dz, density=1e14, v_mean=0.3, v_spread=0.003, seed=20261203,
+              sort=True):
     """Seeded beam: positions uniform over cells [clo, chi), vz ~ N(v_mean c, v_spread c),
-    vx = 0, equal weights giving ``density`` [m^-3]; sorted by position."""
+    vx = 0, equal weights giving ``density`` [m^-3]; sorted by position unless sort=False."""
     rng = np.random.Generator(np.random.PCG64(seed))
     zeta = clo + (chi - clo) * rng.random(n_part)
     vz = rng.normal(v_mean, v_spread, n_part)
     uz = vz / np.sqrt(1.0 - vz * vz)
-    order = np.argsort(zeta, kind="stable")
-    zeta, uz = zeta[order], uz[order]
+    if sort:
+        order = np.argsort(zeta, kind="stable")
+        zeta, uz = zeta[order], uz[order]
     cell = np.floor(zeta).astype(np.int32)
     weight = density * (chi - clo) * dz / max(1, n_part)
     return Beam(cell=cell, frac=zeta - cell, ux=np.zeros(n_part), uz=uz.copy(),

@@ -122,7 +122,7 @@ class Server:
 
     def __init__(self, precision="f32", hbm_budget=150e9, max_active=None, chunk_ms=3.0,
                  threads=512, smem_bytes=64 * 1024, max_inflight=2, keep_state=False,
-                 device=None, clock=time.perf_counter):
+                 max_admit_per_poll=64, device=None, clock=time.perf_counter):
         _require_cuda()
         self.L = lib()
         check_slot_layout(self.L)
@@ -138,6 +138,7 @@ class Server:
         self.max_active = int(max_active or 2 * self.ctas)
         self.chunk_ns = chunk_ms * 1e6
         self.max_inflight = max_inflight
+        self.max_admit = max_admit_per_poll
         self.keep_state = keep_state
         self.clock = clock
         self.stream = torch.cuda.Stream(device=self.dev)
@@ -192,7 +193,7 @@ class Server:
 
     def _admit(self, now):
         admitted = 0
-        while self.pending and self.free:
+        while self.pending and self.free and admitted < self.max_admit:
             req = self.pending[0]
             need = self.request_bytes(req)
             if self.bytes_in_use + need > self.budget and self.active:
@@ -483,7 +484,7 @@ def make_request_stream(rate=2000.0, duration=60.0, seed=20261203, nz_lo=256, nz
         if npart[i] > 0:
             clo, chi, npi, sd = 50, N - 51, int(npart[i]), int(seeds[i])
             r.beam_fn = (lambda npi=npi, clo=clo, chi=chi, sd=sd:
-                         make_beam(npi, clo, chi, dz, seed=sd))
+                         make_beam(npi, clo, chi, dz, seed=sd, sort=False))
             r.n_part = npi
         reqs.append(r)
     return reqs

@@ -127,8 +127,16 @@ class Sweep:
         self.graph = None
 
     def _enqueue(self, stream):
+        self.launch_fields(stream)
+        self.launch_spectra(stream)
+
+    def launch_fields(self, stream):
+        """The persistent batch launch: every instance's steps and probe traces."""
+        engine.launch(self.packed, stream=stream, threads=self.threads, grid_ctas=self.grid_ctas)
+
+    def launch_spectra(self, stream):
+        """DFT of both probe traces of every instance, then |R(f)|."""
         p = self.packed
-        engine.launch(p, stream=stream, threads=self.threads, grid_ctas=self.grid_ctas)
         st = ctypes.c_void_p(stream.cuda_stream)
         check(self.L.fdtdpic_dft_probes(p.prec, engine._ptr(p.d_probe), 2 * self.n, self.S, 2,
                                         2 * self.S, 1, 2, engine._ptr(self.d_tw), self.F,
