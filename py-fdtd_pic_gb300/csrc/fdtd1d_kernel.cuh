@@ -76,6 +76,27 @@ struct Kerr<float> {
     }
 };
 
+// The instance descriptor, copied once per CTA into shared memory.  Kernels read its fields in
+// every cell update; from shared memory those reads neither travel to L2 nor alias the state
+// stores (a per-thread copy would live in local memory, a reference to global memory would be
+// re-read after every store).  Every thread must call it (it holds barriers).
+__device__ inline void copy_instance_block(FdtdInstance &dst, const FdtdInstance &src)
+{
+    static_assert(sizeof(FdtdInstance) % 4 == 0, "FdtdInstance is copied as 32-bit words");
+    __syncthreads();  // an earlier use of dst by this CTA is finished
+    const int *s = reinterpret_cast<const int *>(&src);
+    int *d = reinterpret_cast<int *>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(FdtdInstance) / 4); i += blockDim.x) d[i] = s[i];
+    __syncthreads();
+}
+
+__device__ inline const FdtdInstance &instance_block(const FdtdInstance &src)
+{
+    __shared__ FdtdInstance s_inst;
+    copy_instance_block(s_inst, src);
+    return s_inst;
+}
+
 // Per-launch set-up done once per CTA instead of once per thread: the Kerr constants (folded in
 // FP64, whose pipe is narrow) and the step's source values.  Every thread of the CTA must call
 // these (they hold a barrier).
@@ -124,6 +145,8 @@ struct SmemStore {
     int front, W;
     __device__ T &Ex(int k) { return ex[k]; }
     __device__ T &Hy(int k) { return hy[k]; }
+    __device__ T ExR(int k) { return ex[k]; }  // reads of the field the phase does not write
+    __device__ T HyR(int k) { return hy[k]; }
     __device__ T &Dx(int k) { return dx[k - front]; }
     __device__ T &P(int k) { return p[k - front]; }
     __device__ T &Pp(int k) { return pp[k - front]; }
@@ -132,13 +155,18 @@ struct SmemStore {
     __device__ T tab_at(int row, int col) const { return tab[row * W + col]; }
 };
 
-template <typename T>
+// NC: the kernel holding this store runs one phase only, so the field it reads with ExR/HyR
+// (Ex in the H phase, Hy in the E phase) is read-only for the whole launch and may go through
+// the non-coherent path; such loads also need not wait behind the phase's own stores.
+template <typename T, bool NC = false>
 struct GlobalStore {
     T *ex, *hy, *dx, *p, *pp, *psie, *psih;
     const double *tab;
     int W;
     __device__ T &Ex(int k) { return ex[k]; }
     __device__ T &Hy(int k) { return hy[k]; }
+    __device__ T ExR(int k) const { return NC ? __ldg(ex + k) : ex[k]; }
+    __device__ T HyR(int k) const { return NC ? __ldg(hy + k) : hy[k]; }
     __device__ T &Dx(int k) { return dx[k]; }
     __device__ T &P(int k) { return p[k]; }
     __device__ T &Pp(int k) { return pp[k]; }
@@ -156,7 +184,7 @@ __device__ __forceinline__ void e_cell(const FdtdInstance &I, const Scal<T> &c, 
                                        T *a_out, int *nfb, bool dx_jx = false)
 {
     const int n = I.nz + 1;
-    const T hk = s.Hy(k), hkm = s.Hy(k - 1);
+    const T hk = s.HyR(k), hkm = s.HyR(k - 1);
     T ex = s.Ex(k);
     const bool slab = (k >= I.front) && (k < I.rear);
     if (I.mode == FDTD_MODE_LINLOR && I.pol_active && slab) {
@@ -206,7 +234,7 @@ __device__ __forceinline__ void h_cell(const FdtdInstance &I, const Scal<T> &c, 
     const int n = I.nz + 1;
     T hy = s.Hy(k);
     if (I.tfsf && k == I.nzsrc - 1) hy = hy - src_h;
-    const T exk = s.Ex(k), exk1 = s.Ex(k + 1);
+    const T exk = s.ExR(k), exk1 = s.ExR(k + 1);
     const bool slab = (k >= I.front) && (k < I.rear);
     const int col = pml_col(I, k);
     const T den = (col >= 0) ? s.tab_at(FDTD_TAB_DENH, col) : T(1);
@@ -384,11 +412,12 @@ __global__ void __launch_bounds__(1024) fdtd_batch_kernel(BatchArgs<T> args)
         __syncthreads();
         if (q >= args.n_inst) break;
         const int idx = args.order ? args.order[q] : q;
-        if (resident_elems<T>(args.inst[idx]) * (int64_t)sizeof(T) > args.smem_bytes) {
+        const FdtdInstance &I = instance_block(args.inst[idx]);
+        if (resident_elems<T>(I) * (int64_t)sizeof(T) > args.smem_bytes) {
             if (threadIdx.x == 0 && args.status) atomicOr(args.status + idx, FDTD_STATUS_SKIPPED);
             continue;
         }
-        run_instance_resident<T>(args, args.inst[idx], idx, smem);
+        run_instance_resident<T>(args, I, idx, smem);
         __syncthreads();
     }
 }
@@ -396,12 +425,12 @@ __global__ void __launch_bounds__(1024) fdtd_batch_kernel(BatchArgs<T> args)
 // ---------------------------------------------------------------------------------------
 // global-memory path: one instance of any size, two launches per step
 // ---------------------------------------------------------------------------------------
-template <typename T>
-__device__ inline GlobalStore<T> global_store(const FdtdInstance &I, const BatchArgs<T> &args)
+template <typename T, bool NC = false>
+__device__ inline GlobalStore<T, NC> global_store(const FdtdInstance &I, const BatchArgs<T> &args)
 {
     const int n = I.nz + 1;
     T *gst = args.state + I.state_offset;
-    GlobalStore<T> s;
+    GlobalStore<T, NC> s;
     s.ex = gst + (int64_t)FDTD_ST_EX * n;
     s.hy = gst + (int64_t)FDTD_ST_HY * n;
     s.dx = gst + (int64_t)FDTD_ST_DX * n;
@@ -417,8 +446,8 @@ __device__ inline GlobalStore<T> global_store(const FdtdInstance &I, const Batch
 template <typename T>
 __global__ void __launch_bounds__(256, 4) fdtd_global_e_kernel(BatchArgs<T> args, int t)
 {
-    const FdtdInstance I = args.inst[0];  // by value: fields stay in registers
-    GlobalStore<T> s = global_store<T>(I, args);
+    const FdtdInstance &I = instance_block(args.inst[0]);
+    GlobalStore<T, true> s = global_store<T, true>(I, args);
     const Scal<T> c = scal_block<T>(I);
     Kerr<T> kr;
     kerr_setup_block<T>(kr, I);
@@ -435,8 +464,8 @@ __global__ void __launch_bounds__(256, 4) fdtd_global_e_kernel(BatchArgs<T> args
 template <typename T>
 __global__ void __launch_bounds__(256, 4) fdtd_global_h_kernel(BatchArgs<T> args, int t)
 {
-    const FdtdInstance I = args.inst[0];  // by value: fields stay in registers
-    GlobalStore<T> s = global_store<T>(I, args);
+    const FdtdInstance &I = instance_block(args.inst[0]);
+    GlobalStore<T, true> s = global_store<T, true>(I, args);
     const Scal<T> c = scal_block<T>(I);
     const double *Hys = args.src + I.src_offset + I.n_steps;
     const T src_h = I.tfsf ? (T)(Hys[t] / I.sc) : T(0);
@@ -450,7 +479,7 @@ __global__ void __launch_bounds__(256, 4) fdtd_global_h_kernel(BatchArgs<T> args
 template <typename T>
 __global__ void fdtd_global_probe_kernel(BatchArgs<T> args, int t)
 {
-    const FdtdInstance I = args.inst[0];  // by value: fields stay in registers
+    const FdtdInstance &I = instance_block(args.inst[0]);
     const int n = I.nz + 1;
     const T *ex = args.state + I.state_offset + (int64_t)FDTD_ST_EX * n;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -467,7 +496,7 @@ __global__ void fdtd_global_probe_kernel(BatchArgs<T> args, int t)
 template <typename T>
 __global__ void fdtd_global_init_kernel(BatchArgs<T> args)
 {
-    const FdtdInstance I = args.inst[0];  // by value: fields stay in registers
+    const FdtdInstance &I = instance_block(args.inst[0]);
     const int64_t n = (int64_t)I.nz + 1;
     T *gst = args.state + I.state_offset;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < FDTD_STATE_ARRAYS * n;
@@ -478,7 +507,7 @@ __global__ void fdtd_global_init_kernel(BatchArgs<T> args)
 template <typename T>
 __global__ void fdtd_global_finish_kernel(BatchArgs<T> args)
 {
-    const FdtdInstance I = args.inst[0];  // by value: fields stay in registers
+    const FdtdInstance &I = instance_block(args.inst[0]);
     const int n = I.nz + 1;
     const T *gst = args.state + I.state_offset;
     bool bad = false;

@@ -295,30 +295,37 @@ __device__ __forceinline__ int pic_step_index(const PicField<T> &a, int t)
 
 // E phase of cell k with the beam: Hyp <- Hy (H^(t+1/2) for the next push), currents out of the
 // accumulators (which are zeroed for the next push), then the reference E phase with -Jx.
-template <typename T>
-__device__ __forceinline__ void pic_e_cell(PicField<T> &a, const FdtdInstance &I,
-                                           GlobalStore<T> &s, const Scal<T> &c, const Kerr<T> &kr,
-                                           int k, int n, T src_e, T src_h, T *gA, int *nfb)
+// Loads first (the accumulator words, then e_cell's field reads), stores after: the cell's
+// loads then go out together instead of each waiting behind an earlier store.
+template <typename T, class S>
+__device__ __forceinline__ void pic_e_cell(PicField<T> &a, const FdtdInstance &I, S &s,
+                                           const Scal<T> &c, const Kerr<T> &kr, int k, int n,
+                                           T src_e, T src_h, T *gA, int *nfb)
 {
     constexpr int W = Fix<T>::W;
-    a.hyp[k] = s.Hy(k);
     unsigned long long wx[W], wz[W];
 #pragma unroll
     for (int w = 0; w < W; ++w) {
         wx[w] = a.acc[(size_t)w * n + k];
         wz[w] = a.acc[(size_t)(W + w) * n + k];
+    }
+    const T hyk = s.HyR(k);
+    const T jxk = Fix<T>::join(wx, a.jinv, a.jinv_f);
+    const T jzk = Fix<T>::join(wz, a.jinv, a.jinv_f);
+    if (k >= 1) e_cell<T>(I, c, kr, s, k, src_e, src_h, true, jxk, gA, nfb, true);
+    a.hyp[k] = hyk;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
         a.acc[(size_t)w * n + k] = 0ull;
         a.acc[(size_t)(W + w) * n + k] = 0ull;
     }
-    const T jxk = Fix<T>::join(wx, a.jinv, a.jinv_f);
     a.jx[k] = jxk;
-    a.jz[k] = Fix<T>::join(wz, a.jinv, a.jinv_f);
-    if (k >= 1) e_cell<T>(I, c, kr, s, k, src_e, src_h, true, jxk, gA, nfb, true);
+    a.jz[k] = jzk;
 }
 
-template <typename T>
-__device__ __forceinline__ void pic_probes(PicField<T> &a, const FdtdInstance &I,
-                                           GlobalStore<T> &s, int t, int gt, int gstride, int n)
+template <typename T, class S>
+__device__ __forceinline__ void pic_probes(PicField<T> &a, const FdtdInstance &I, S &s, int t,
+                                           int gt, int gstride, int n)
 {
     if (gt < 2 && t >= I.probe_lo[gt] && t <= I.probe_hi[gt])
         a.f.probe[I.probe_offset + (int64_t)t * 2 + gt] = s.Ex(I.probe_cell[gt]);
@@ -333,9 +340,9 @@ __device__ __forceinline__ void pic_probes(PicField<T> &a, const FdtdInstance &I
 template <typename T>
 __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
 {
-    const FdtdInstance I = a.f.inst[0];  // by value: fields stay in registers
+    const FdtdInstance &I = instance_block(a.f.inst[0]);
     const int t = pic_step_index(a, t_arg);
-    GlobalStore<T> s = global_store<T>(I, a.f);
+    GlobalStore<T, true> s = global_store<T, true>(I, a.f);
     const Scal<T> c = scal_block<T>(I);
     Kerr<T> kr;
     kerr_setup_block<T>(kr, I);
@@ -352,9 +359,9 @@ __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
 template <typename T>
 __global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
 {
-    const FdtdInstance I = a.f.inst[0];  // by value: fields stay in registers
+    const FdtdInstance &I = instance_block(a.f.inst[0]);
     const int t = pic_step_index(a, t_arg);
-    GlobalStore<T> s = global_store<T>(I, a.f);
+    GlobalStore<T, true> s = global_store<T, true>(I, a.f);
     const Scal<T> c = scal_block<T>(I);
     const T src_h = I.tfsf ? (T)(a.f.src[I.src_offset + I.n_steps + t] / I.sc) : T(0);
     const int n = I.nz + 1;
@@ -375,7 +382,7 @@ template <typename T>
 __global__ void __launch_bounds__(1024) pic_field_fused_kernel(PicField<T> a, int32_t *step_w,
                                                                 int t_arg)
 {
-    const FdtdInstance I = a.f.inst[0];  // by value: fields stay in registers
+    const FdtdInstance &I = instance_block(a.f.inst[0]);
     const int t = pic_step_index(a, t_arg);
     GlobalStore<T> s = global_store<T>(I, a.f);
     const Scal<T> c = scal_block<T>(I);

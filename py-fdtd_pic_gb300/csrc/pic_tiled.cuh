@@ -114,6 +114,8 @@ struct TileStore {
     int base, c0, W;
     __device__ T &Ex(int k) { return ex[k - base]; }
     __device__ T &Hy(int k) { return hy[k - base]; }
+    __device__ T ExR(int k) { return ex[k - base]; }
+    __device__ T HyR(int k) { return hy[k - base]; }
     __device__ T &Dx(int k) { return dx[k - c0]; }
     __device__ T &P(int k) { return p[k - c0]; }
     __device__ T &Pp(int k) { return pp[k - c0]; }
@@ -139,7 +141,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 1) pic_tiled_kernel(TileArgs<T> 
     __shared__ T s_src[2];
     const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
     const int warp = tid >> 5;
-    const FdtdInstance I = a.f.inst[0];
+    const FdtdInstance &I = instance_block(a.f.inst[0]);
     const int n = I.nz + 1;
     const int c0 = tile_begin(b, a.G, n);
     const int c1 = tile_begin(b + 1, a.G, n);

@@ -239,14 +239,19 @@ __global__ void __launch_bounds__(1024) fdtdpic_slot_kernel(SlotArgs a)
         const FdtdSlotItem it = a.items[q];
         if (it.slot < 0 || it.slot >= a.n_slots) continue;
         FdtdSlot &S = a.slots[it.slot];
-        FdtdInstance I = S.inst;
+        __shared__ FdtdInstance s_inst;
+        copy_instance_block(s_inst, S.inst);
+        const FdtdInstance &I = s_inst;
         if (it.t0 < 0 || it.t1 < it.t0 || it.t1 > I.n_steps) {
             if (threadIdx.x == 0) atomicOr(&S.status[1], FDTD_STATUS_SKIPPED);
             continue;
         }
-        I.step_begin = it.t0;
-        I.step_end = it.t1;
-        I.resume = it.first ? 0 : 1;
+        if (threadIdx.x == 0) {
+            s_inst.step_begin = it.t0;
+            s_inst.step_end = it.t1;
+            s_inst.resume = it.first ? 0 : 1;
+        }
+        __syncthreads();
         if (S.n_part > 0) {
             run_beam_slot<T>(S, I, smem_raw, a.smem_bytes);
         } else {

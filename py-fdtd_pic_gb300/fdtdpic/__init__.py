@@ -3,8 +3,9 @@
 Host-side entry points:
   fdtdpic.engine.run(grids, precision)      run grids (one launch for all resident grids)
   fdtdpic.grid.grids_from_reference(...)    grids of a reference integrator call
-The reference-compatible modules (Solver_Engine, BaseFDTD11, MasterController, ...) live one
-directory up and call into this package.
+  fdtdpic.sweep / fdtdpic.pic / fdtdpic.server  batched sweeps, beam PIC, served requests
+The reference-compatible modules (MasterController, Solver_Engine, BaseFDTD11, ...) are in
+fdtdpic.compat and call into this package.
 """
 from ._lib import build, lib  # noqa: F401
 
