@@ -177,6 +177,13 @@ int fdtdpic_dft_twiddles(const double *d_freqs, int F, int S, double dt, void *d
 int fdtdpic_dft_probes(int precision, const void *d_traces, int R, int S, int rp, int64_t ldp,
                        int64_t sp, int64_t sn, const void *d_tw, int F, double *d_out,
                        fdtdpic_stream_t stream);
+/* The same X on the tensor cores (tcgen05, sm_103a): split-BF16x3 products (about 16
+ * significant bits each) with FP32 sums over 64-step chunks in tensor memory and FP64 sums
+ * across chunks.  d_err (one int32, caller-zeroed) is set non-zero if a bounded wait for the
+ * tensor cores gave up (the affected outputs are then not written). */
+int fdtdpic_dft_probes_tc(int precision, const void *d_traces, int R, int S, int rp, int64_t ldp,
+                          int64_t sp, int64_t sn, const void *d_tw, int F, double *d_out,
+                          int32_t *d_err, fdtdpic_stream_t stream);
 /* |R(f)| = |X[2p+1, f]| / |X[2p, f]| for n_pairs trace pairs (0 where |X[2p, f]| = 0). */
 int fdtdpic_reflection_ratio(const double *d_X, int n_pairs, int F, double *d_ratio,
                              fdtdpic_stream_t stream);
@@ -303,6 +310,9 @@ int fdtdpic_slot_check(int precision, const FdtdSlot *slot);
 /* Shared memory (bytes) with which this slot's fields (field-only request) or deposit
  * accumulators (beam request) stay on chip; host-only. */
 int64_t fdtdpic_slot_smem_bytes(int precision, const FdtdSlot *slot);
+/* CTAs one fdtdpic_slots_run launch keeps resident with these settings (grid_ctas <= 0 picks
+ * this many); 0 when the settings are invalid or no device is usable. */
+int fdtdpic_slots_grid(int precision, int64_t smem_bytes, int threads_per_cta);
 /* Run n_items work items over n_slots slots (both arrays in device memory) in one launch.
  * d_queue: one int32 of caller scratch, reset by this call.  smem_bytes: dynamic shared memory
  * per CTA (items whose slot needs more run from global memory).  threads_per_cta <= 0 picks

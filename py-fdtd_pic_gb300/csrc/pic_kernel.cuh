@@ -236,9 +236,10 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
             int j;
             T fh;
             if (f >= T(0.5)) { j = c; fh = f - T(0.5); } else { j = c - 1; fh = f + T(0.5); }
-            const T E = (T(1) - f) * a.ex[c] + f * a.ex[c + 1];
-            const T H = (T(1) - fh) * (T(0.5) * (a.hy[j] + a.hyp[j])) +
-                        fh * (T(0.5) * (a.hy[j + 1] + a.hyp[j + 1]));
+            // the fields are read-only during the push: non-coherent loads
+            const T E = (T(1) - f) * __ldg(a.ex + c) + f * __ldg(a.ex + c + 1);
+            const T H = (T(1) - fh) * (T(0.5) * (__ldg(a.hy + j) + __ldg(a.hyp + j))) +
+                        fh * (T(0.5) * (__ldg(a.hy + j + 1) + __ldg(a.hyp + j + 1)));
             Moved<T> m;
             particle_step<T>(E, H, c, f, a.ux[p], a.uz[p], a.kE, a.kH, a.sc, a.kJ, a.kJz, m);
             const T uxn = m.ux, uzn = m.uz, f1 = m.f1;
@@ -277,14 +278,49 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
     }
 }
 
+// The instance's update constants in the state type and its folded FP32 Kerr constants,
+// computed once per call by pic_consts_kernel (the FP64 pipe is narrow; the field kernels then
+// do no FP64 set-up of their own).
+template <typename T>
+struct FieldConsts {
+    Scal<T> c;
+    Kerr<T> kr;
+};
+
+template <typename T>
+__global__ void pic_consts_kernel(const FdtdInstance *inst, FieldConsts<T> *out)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        out->c = make_scal<T>(*inst);
+        out->kr.setup(*inst);
+    }
+}
+
+// Copy the call's constants into shared memory once per CTA (every thread calls it).
+template <typename T>
+__device__ inline void consts_block(const FieldConsts<T> *g, Scal<T> &c, Kerr<T> &kr)
+{
+    static_assert(sizeof(FieldConsts<T>) % 4 == 0, "FieldConsts is copied as 32-bit words");
+    __shared__ FieldConsts<T> s_fc;
+    __syncthreads();
+    const int *src = reinterpret_cast<const int *>(g);
+    int *dst = reinterpret_cast<int *>(&s_fc);
+    for (int i = threadIdx.x; i < (int)(sizeof(FieldConsts<T>) / 4); i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    c = s_fc.c;
+    kr = s_fc.kr;
+}
+
 template <typename T>
 struct PicField {
     BatchArgs<T> f;
+    const FieldConsts<T> *fc;
     unsigned long long *acc;
     T *jx, *jz, *hyp;
     double jinv;
     float jinv_f;
     const int32_t *step;  // device step counter (graph replay); NULL: use the launch argument
+    int last;             // the call's last step: Jz was deposited, Jz and Acubic are written out
 };
 
 template <typename T>
@@ -296,7 +332,9 @@ __device__ __forceinline__ int pic_step_index(const PicField<T> &a, int t)
 // E phase of cell k with the beam: Hyp <- Hy (H^(t+1/2) for the next push), currents out of the
 // accumulators (which are zeroed for the next push), then the reference E phase with -Jx.
 // Loads first (the accumulator words, then e_cell's field reads), stores after: the cell's
-// loads then go out together instead of each waiting behind an earlier store.
+// loads then go out together instead of each waiting behind an earlier store.  Jz words are
+// only non-zero on the call's last step (the only step that deposits them), so they are read,
+// cleared and written out then, with the Acubic diagnostic; every other step skips them.
 template <typename T, class S>
 __device__ __forceinline__ void pic_e_cell(PicField<T> &a, const FdtdInstance &I, S &s,
                                            const Scal<T> &c, const Kerr<T> &kr, int k, int n,
@@ -307,20 +345,20 @@ __device__ __forceinline__ void pic_e_cell(PicField<T> &a, const FdtdInstance &I
 #pragma unroll
     for (int w = 0; w < W; ++w) {
         wx[w] = a.acc[(size_t)w * n + k];
-        wz[w] = a.acc[(size_t)(W + w) * n + k];
+        wz[w] = a.last ? a.acc[(size_t)(W + w) * n + k] : 0ull;
     }
     const T hyk = s.HyR(k);
     const T jxk = Fix<T>::join(wx, a.jinv, a.jinv_f);
-    const T jzk = Fix<T>::join(wz, a.jinv, a.jinv_f);
-    if (k >= 1) e_cell<T>(I, c, kr, s, k, src_e, src_h, true, jxk, gA, nfb, true);
+    if (k >= 1) e_cell<T>(I, c, kr, s, k, src_e, src_h, true, jxk, a.last ? gA : nullptr, nfb, true);
     a.hyp[k] = hyk;
 #pragma unroll
-    for (int w = 0; w < W; ++w) {
-        a.acc[(size_t)w * n + k] = 0ull;
-        a.acc[(size_t)(W + w) * n + k] = 0ull;
-    }
+    for (int w = 0; w < W; ++w) a.acc[(size_t)w * n + k] = 0ull;
     a.jx[k] = jxk;
-    a.jz[k] = jzk;
+    if (a.last) {
+#pragma unroll
+        for (int w = 0; w < W; ++w) a.acc[(size_t)(W + w) * n + k] = 0ull;
+        a.jz[k] = Fix<T>::join(wz, a.jinv, a.jinv_f);
+    }
 }
 
 template <typename T, class S>
@@ -343,9 +381,9 @@ __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
     const FdtdInstance &I = instance_block(a.f.inst[0]);
     const int t = pic_step_index(a, t_arg);
     GlobalStore<T, true> s = global_store<T, true>(I, a.f);
-    const Scal<T> c = scal_block<T>(I);
+    Scal<T> c;
     Kerr<T> kr;
-    kerr_setup_block<T>(kr, I);
+    consts_block<T>(a.fc, c, kr);
     T src_e, src_h;
     source_block<T>(I, a.f.src + I.src_offset, t, src_e, src_h);
     const int n = I.nz + 1;
@@ -362,7 +400,9 @@ __global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
     const FdtdInstance &I = instance_block(a.f.inst[0]);
     const int t = pic_step_index(a, t_arg);
     GlobalStore<T, true> s = global_store<T, true>(I, a.f);
-    const Scal<T> c = scal_block<T>(I);
+    Scal<T> c;
+    Kerr<T> kr;
+    consts_block<T>(a.fc, c, kr);
     const T src_h = I.tfsf ? (T)(a.f.src[I.src_offset + I.n_steps + t] / I.sc) : T(0);
     const int n = I.nz + 1;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -385,9 +425,9 @@ __global__ void __launch_bounds__(1024) pic_field_fused_kernel(PicField<T> a, in
     const FdtdInstance &I = instance_block(a.f.inst[0]);
     const int t = pic_step_index(a, t_arg);
     GlobalStore<T> s = global_store<T>(I, a.f);
-    const Scal<T> c = scal_block<T>(I);
+    Scal<T> c;
     Kerr<T> kr;
-    kerr_setup_block<T>(kr, I);
+    consts_block<T>(a.fc, c, kr);
     T src_e, src_h;
     source_block<T>(I, a.f.src + I.src_offset, t, src_e, src_h);
     const int n = I.nz + 1;
@@ -529,7 +569,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Scratch layout shared by the size query and the launcher.
 struct PicScratch {
-    size_t acc, counts, cursor, step, tile_sum, cell2, frac2, ux2, uz2, id2, total;
+    size_t acc, counts, cursor, step, tile_sum, consts, cell2, frac2, ux2, uz2, id2, total;
 };
 inline PicScratch pic_scratch_layout(int tsize, int nz, int n_part)
 {
@@ -542,6 +582,7 @@ inline PicScratch pic_scratch_layout(int tsize, int nz, int n_part)
     L.cursor = o; o = align256(o + (nz1 + 1) * 4);
     L.step = o; o = align256(o + 4);
     L.tile_sum = o; o = align256(o + ((nz1 + SCAN_TILE - 1) / SCAN_TILE + 1) * 4);
+    L.consts = o; o = align256(o + sizeof(FieldConsts<double>));
     L.cell2 = o; o = align256(o + (size_t)n_part * 4);
     L.frac2 = o; o = align256(o + (size_t)n_part * tsize);
     L.ux2 = o; o = align256(o + (size_t)n_part * tsize);
@@ -623,6 +664,7 @@ void pic_enqueue_step(PicPlan<T> &P, const PicBeam &bm, int t, bool do_sort, boo
     }
     PicField<T> pf = P.pf;
     pf.step = device_step ? P.step : nullptr;
+    pf.last = last_step ? 1 : 0;
     if (tm) tm->begin(&tm->out->field_ms);
     if (P.fused) {
         pic_field_fused_kernel<T><<<1, 1024, 0, st>>>(pf, device_step ? P.step : nullptr, t);
@@ -686,7 +728,8 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
     pa.acc = acc;
     pa.status = status;
     P.pf.f = fa; P.pf.acc = acc; P.pf.jx = jx; P.pf.jz = jz; P.pf.hyp = hyp;
-    P.pf.jinv = pa.jinv; P.pf.jinv_f = pa.jinv_f; P.pf.step = nullptr;
+    P.pf.jinv = pa.jinv; P.pf.jinv_f = pa.jinv_f; P.pf.step = nullptr; P.pf.last = 0;
+    P.pf.fc = (const FieldConsts<T> *)(scratch + L.consts);
     P.pblocks = (bm.n_part + pa.chunk - 1) / pa.chunk;
     P.sblocks = (bm.n_part + P.threads - 1) / P.threads;
     if (P.sblocks > 16 * sms) P.sblocks = 16 * sms;
@@ -695,6 +738,7 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
     cudaError_t e = cudaMemsetAsync(acc, 0, (size_t)2 * W * nz1 * 8, st);
     if (e != cudaSuccess) return cuda_status(e);
     if (!h.resume) fdtd_global_init_kernel<T><<<P.fblocks, P.threads, 0, st>>>(fa);
+    pic_consts_kernel<T><<<1, 32, 0, st>>>(fa.inst, (FieldConsts<T> *)(scratch + L.consts));
 
     PicTimer tmr{timing, st, {nullptr, nullptr}, 0, nullptr};
     if (timing) {

@@ -8,6 +8,20 @@ namespace fdtdpic {
 
 int check_instance(const FdtdInstance &I);
 
+// CTAs per SM the slot kernel runs at with this block size and shared memory (0 on error).
+template <typename T>
+static int slots_per_sm(int threads, int64_t smem_bytes)
+{
+    int per_sm = 0;
+    if (cudaFuncSetAttribute(fdtdpic_slot_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_bytes) != cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fdtdpic_slot_kernel<T>, threads,
+                                                      (size_t)smem_bytes) != cudaSuccess)
+        return 0;
+    return per_sm;
+}
+
 template <typename T>
 static int launch_slots(const SlotArgs &a, int threads, int grid, cudaStream_t st)
 {
@@ -91,6 +105,21 @@ int64_t fdtdpic_slot_smem_bytes(int precision, const FdtdSlot *s)
     if (s->n_part > 0) return 2 * (precision == FDTDPIC_F64 ? 2 : 1) * n * 8;
     return precision == FDTDPIC_F64 ? resident_elems<double>(s->inst) * 8
                                     : resident_elems<float>(s->inst) * 4;
+}
+
+int fdtdpic_slots_grid(int precision, int64_t smem_bytes, int threads_per_cta)
+{
+    int dev = 0, sms = 0, max_optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (smem_bytes < 0 || smem_bytes > (int64_t)max_optin - 1024) return 0;
+    if (threads_per_cta <= 0) threads_per_cta = 512;
+    if (threads_per_cta > 1024 || (threads_per_cta % 32) != 0) return 0;
+    int per_sm = 0;
+    if (precision == FDTDPIC_F64) per_sm = slots_per_sm<double>(threads_per_cta, smem_bytes);
+    else if (precision == FDTDPIC_F32) per_sm = slots_per_sm<float>(threads_per_cta, smem_bytes);
+    return per_sm * sms;
 }
 
 int fdtdpic_slots_run(int precision, FdtdSlot *d_slots, int n_slots, const FdtdSlotItem *d_items,

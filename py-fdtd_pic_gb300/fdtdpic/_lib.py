@@ -28,6 +28,7 @@ UNITS = {
     "pic_f64.cu": ["-fmad=false"],
     "pic_f32.cu": ["-fmad=false"],  # PIC paths agree bit for bit (explicit fmaf in the push)
     "dft.cu": [],
+    "dft_tc.cu": [],
     "slot.cu": ["-fmad=false"],  # beam requests round as fdtdpic_run's step
     "noalloc.cu": [],
 }
@@ -151,6 +152,9 @@ def _declare(L):
     L.fdtdpic_dft_probes.restype = c_int
     L.fdtdpic_dft_probes.argtypes = [c_int, P, c_int, c_int, c_int, c_i64, c_i64, c_i64, P,
                                      c_int, P, P]
+    L.fdtdpic_dft_probes_tc.restype = c_int
+    L.fdtdpic_dft_probes_tc.argtypes = [c_int, P, c_int, c_int, c_int, c_i64, c_i64, c_i64, P,
+                                        c_int, P, P, P]
     L.fdtdpic_reflection_ratio.restype = c_int
     L.fdtdpic_reflection_ratio.argtypes = [P, c_int, c_int, P, P]
     L.fdtdpic_slot_layout.restype = c_int
@@ -159,6 +163,8 @@ def _declare(L):
     L.fdtdpic_slot_check.argtypes = [c_int, P]
     L.fdtdpic_slot_smem_bytes.restype = c_i64
     L.fdtdpic_slot_smem_bytes.argtypes = [c_int, P]
+    L.fdtdpic_slots_grid.restype = c_int
+    L.fdtdpic_slots_grid.argtypes = [c_int, c_i64, c_int]
     L.fdtdpic_slots_run.restype = c_int
     L.fdtdpic_slots_run.argtypes = [c_int, P, c_int, P, c_int, P, c_i64, c_int, c_int, P]
     L.fdtdpic_run_noalloc.restype = c_int

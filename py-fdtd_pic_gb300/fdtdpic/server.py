@@ -22,6 +22,8 @@ from __future__ import annotations
 import collections
 import ctypes
 import math
+import queue
+import threading
 import time
 from dataclasses import dataclass, field
 
@@ -122,7 +124,7 @@ class Server:
 
     def __init__(self, precision="f32", hbm_budget=150e9, max_active=None, chunk_ms=3.0,
                  threads=512, smem_bytes=64 * 1024, max_inflight=2, keep_state=False,
-                 max_admit_per_poll=64, device=None, clock=time.perf_counter):
+                 max_admit_per_poll=64, prefetch=128, device=None, clock=time.perf_counter):
         _require_cuda()
         self.L = lib()
         check_slot_layout(self.L)
@@ -132,9 +134,9 @@ class Server:
         self.budget = float(hbm_budget)
         self.threads = threads
         self.smem = int(smem_bytes)
-        props = torch.cuda.get_device_properties(self.dev)
-        per_sm = max(1, min(2048 // threads, (228 * 1024) // (self.smem + 1024)))
-        self.ctas = per_sm * props.multi_processor_count
+        self.ctas = int(self.L.fdtdpic_slots_grid(self.prec, self.smem, threads))
+        if self.ctas <= 0:
+            raise ValueError(f"no slot kernel launch fits threads={threads}, smem={smem_bytes}")
         self.max_active = int(max_active or 2 * self.ctas)
         self.chunk_ns = chunk_ms * 1e6
         self.max_inflight = max_inflight
@@ -149,7 +151,15 @@ class Server:
         self.d_queue = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self.free = list(range(n - 1, -1, -1))
         self.active: dict[int, _Active] = {}
-        self.pending: collections.deque = collections.deque()
+        # admission pipeline: submitted -> prepared on the host by a worker thread (grid, beam,
+        # pinned staging copies) -> admitted into a slot by the scheduling thread
+        self._inbox: queue.Queue = queue.Queue()
+        self._ready: collections.deque = collections.deque()
+        self._ready_cv = threading.Condition()
+        self._prefetch = max(1, int(prefetch))
+        self._unadmitted = 0
+        self._worker = threading.Thread(target=self._prepare_loop, daemon=True)
+        self._worker.start()
         self.bytes_in_use = 0
         self.inflight: collections.deque = collections.deque()
         self.done: list[Done] = []
@@ -188,54 +198,99 @@ class Server:
                                                       self.prec) or (1 << 40))
 
     # ---- admission ----------------------------------------------------------------------------
+    @property
+    def pending(self) -> int:
+        """Requests submitted and not yet admitted."""
+        return self._unadmitted
+
     def submit(self, req: Request):
-        self.pending.append(req)
+        self._unadmitted += 1
+        self._inbox.put(req)
+
+    def close(self):
+        """Stop the preparation thread (pending requests are dropped)."""
+        self._inbox.put(None)
+        with self._ready_cv:
+            self._ready_cv.notify_all()
+
+    def _prepare_loop(self):
+        ts = 8 if self.prec == F64 else 4
+        tdt_np = np.float64 if self.prec == F64 else np.float32
+        while True:
+            req = self._inbox.get()
+            if req is None:
+                return
+            with self._ready_cv:
+                while len(self._ready) >= self._prefetch:
+                    self._ready_cv.wait(0.05)
+            try:
+                if req.grid is None:
+                    req.grid = req.grid_fn()
+                if req.beam is None and req.beam_fn is not None:
+                    req.beam = req.beam_fn()
+                pk = pack([req.grid], ts)
+                host = dict(desc=pk["desc"][0].copy(), n_state=pk["n_state"],
+                            n_probe=pk["n_probe"],
+                            table=torch.from_numpy(pk["table"]).pin_memory(),
+                            src=torch.from_numpy(pk["src"]).pin_memory())
+                b = req.beam
+                if b is not None and b.n > 0:
+                    for k, a, dt_ in (("cell", b.cell, np.int32), ("frac", b.frac, tdt_np),
+                                      ("ux", b.ux, tdt_np), ("uz", b.uz, tdt_np)):
+                        host[k] = torch.from_numpy(np.ascontiguousarray(a, dtype=dt_)).pin_memory()
+                req._host = host
+                req._error = None
+            except Exception as e:  # reported when the request reaches admission
+                req._host, req._error = None, e
+            with self._ready_cv:
+                self._ready.append(req)
+                self._ready_cv.notify_all()
 
     def _admit(self, now):
         admitted = 0
-        while self.pending and self.free and admitted < self.max_admit:
-            req = self.pending[0]
-            need = self.request_bytes(req)
-            if self.bytes_in_use + need > self.budget and self.active:
-                break
-            self.pending.popleft()
+        while self.free and admitted < self.max_admit:
+            with self._ready_cv:
+                if not self._ready:
+                    break
+                req = self._ready[0]
+                need = self.request_bytes(req)
+                if self.bytes_in_use + need > self.budget and self.active:
+                    break
+                self._ready.popleft()
+                self._ready_cv.notify_all()
+            self._unadmitted -= 1
+            if req._error is not None:
+                raise req._error
             self._place(req, need, now)
             admitted += 1
         return admitted
 
     def _place(self, req: Request, need: int, now: float):
-        if req.grid is None:
-            req.grid = req.grid_fn()
-        if req.beam is None and req.beam_fn is not None:
-            req.beam = req.beam_fn()
         g = req.grid
-        ts, tdt, dev = (8 if self.prec == F64 else 4), self.tdt, self.dev
+        host = req._host
+        tdt, dev = self.tdt, self.dev
         n = g.nz + 1
         slot = self.free.pop()
         with torch.cuda.stream(self.stream):
-            pk = pack([g], ts)
-            desc = pk["desc"][0].copy()
+            desc = host["desc"]
             desc["step_begin"], desc["step_end"], desc["resume"] = 0, g.n_steps, 0
-            bufs = dict(
-                table=torch.from_numpy(pk["table"]).pin_memory().to(dev, non_blocking=True),
-                src=torch.from_numpy(pk["src"]).pin_memory().to(dev, non_blocking=True),
-                state=torch.empty(pk["n_state"], dtype=tdt, device=dev),
-                probe=torch.zeros(pk["n_probe"], dtype=tdt, device=dev))
+            bufs = dict(table=host["table"].to(dev, non_blocking=True),
+                        src=host["src"].to(dev, non_blocking=True),
+                        state=torch.empty(host["n_state"], dtype=tdt, device=dev),
+                        probe=torch.zeros(host["n_probe"], dtype=tdt, device=dev))
             s = self.slots_np[slot:slot + 1]  # a view: assignments land in the pinned table
             s[...] = np.zeros(1, SLOT_DTYPE)
             s["inst"] = desc
             s["pml_tab"], s["src"] = bufs["table"].data_ptr(), bufs["src"].data_ptr()
             s["state"], s["probe"] = bufs["state"].data_ptr(), bufs["probe"].data_ptr()
             n_part = 0
-            if req.beam is not None and req.beam.n > 0:
+            if "cell" in host:
                 b = req.beam
                 n_part = b.n
-
-                def up(a, dt_):
-                    return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().to(
-                        dev, dtype=dt_, non_blocking=True)
-                bufs.update(cell=up(b.cell.astype(np.int32), torch.int32), frac=up(b.frac, tdt),
-                            ux=up(b.ux, tdt), uz=up(b.uz, tdt),
+                bufs.update(cell=host["cell"].to(dev, non_blocking=True),
+                            frac=host["frac"].to(dev, non_blocking=True),
+                            ux=host["ux"].to(dev, non_blocking=True),
+                            uz=host["uz"].to(dev, non_blocking=True),
                             hyp=torch.empty(n, dtype=tdt, device=dev),
                             jx=torch.empty(n, dtype=tdt, device=dev),
                             jz=torch.empty(n, dtype=tdt, device=dev),
@@ -259,6 +314,7 @@ class Server:
             sz = SLOT_DTYPE.itemsize
             self.d_slots[slot * sz:(slot + 1) * sz].copy_(
                 self.h_slots[slot * sz:(slot + 1) * sz], non_blocking=True)
+        req._host = None  # the staging copies are released once the copies have run
         self.bytes_in_use += need
         self.active[slot] = _Active(req=req, slot=slot, bufs=bufs, nbytes=need, next_step=0,
                                     cost_ns=self._step_cost_ns(g, n_part), admitted=now)
@@ -386,6 +442,10 @@ class Server:
             self.poll()
             if not self.active and not self.pending:
                 self._complete(block=True)
+            elif not self.active and not self.inflight:
+                with self._ready_cv:  # waiting for the preparation thread
+                    if not self._ready:
+                        self._ready_cv.wait(0.01)
         return self.done
 
     def run_stream(self, requests, duration):
@@ -410,6 +470,10 @@ class Server:
                 time.sleep(min(1e-3, max(0.0, reqs[i].arrival - now)))
                 continue
             self.poll()
+            if not self.active and not self.inflight:
+                with self._ready_cv:  # waiting for the preparation thread
+                    if not self._ready:
+                        self._ready_cv.wait(0.005)
         elapsed = self.clock() - t_start
         self._complete(block=False)
         return self.stats(elapsed, submitted=i)
@@ -421,7 +485,7 @@ class Server:
         return dict(completed=len(self.done), submitted=submitted, elapsed_s=elapsed,
                     throughput_rps=len(self.done) / elapsed if elapsed > 0 else 0.0,
                     p50_s=pct(lat, 50), p99_s=pct(lat, 99), service_p50_s=pct(svc, 50),
-                    service_p99_s=pct(svc, 99), queue_depth=len(self.pending),
+                    service_p99_s=pct(svc, 99), queue_depth=self.pending,
                     active=len(self.active), rounds=self.rounds,
                     mcell_steps_per_s=self.cell_steps / elapsed / 1e6 if elapsed > 0 else 0.0,
                     mparticle_steps_per_s=self.particle_steps / elapsed / 1e6

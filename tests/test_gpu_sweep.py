@@ -59,6 +59,42 @@ def test_dft_matches_numpy_strided(precision):
     np.testing.assert_allclose(ratio, want_r, rtol=1e-4)
 
 
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_dft_tensor_cores_match_numpy(precision):
+    """tcgen05 split-BF16x3 form: each product carries ~16 significant bits, so the error is
+    bounded by ~3 * 2^-17 of the sum of |terms|; FP64 sums across 64-step chunks."""
+    torch = _torch()
+    import ctypes
+    from fdtdpic import engine
+    from fdtdpic._lib import check, lib
+    L = lib()
+    rng = np.random.default_rng(11)
+    n_pairs, S, F = 70, 1000, 77  # 140 traces: two row tiles, the second ragged
+    dt = 2.5e-11
+    freqs = np.sort(rng.uniform(0.1e9, 3.1e9, F))
+    x = rng.standard_normal((n_pairs, S, 2))
+    tdt = torch.float32 if precision == "f32" else torch.float64
+    d_x = torch.from_numpy(x).to(tdt).cuda().contiguous()
+    d_f = torch.from_numpy(freqs).cuda()
+    d_tw = torch.empty(int(L.fdtdpic_dft_twiddle_bytes(F, S)), dtype=torch.uint8, device="cuda")
+    d_out = torch.full((2 * n_pairs * F * 2,), float("nan"), dtype=torch.float64, device="cuda")
+    d_err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    check(L.fdtdpic_dft_twiddles(engine._ptr(d_f), F, S, dt, engine._ptr(d_tw), st))
+    prec = 4 if precision == "f32" else 8
+    check(L.fdtdpic_dft_probes_tc(prec, engine._ptr(d_x), 2 * n_pairs, S, 2, 2 * S, 1, 2,
+                                  engine._ptr(d_tw), F, engine._ptr(d_out), engine._ptr(d_err),
+                                  st))
+    torch.cuda.synchronize()
+    assert int(d_err.item()) == 0
+    got = d_out.cpu().numpy().reshape(2 * n_pairs, F, 2)
+    got = got[..., 0] + 1j * got[..., 1]
+    traces = d_x.double().cpu().numpy().transpose(0, 2, 1).reshape(2 * n_pairs, S)
+    want = _np_dft(traces, freqs, dt)
+    err = np.abs(got - want).max() / np.abs(traces).sum(axis=1).max()
+    assert err < 5e-5, err
+
+
 def test_dft_rejects_bad_arguments():
     torch = _torch()
     from fdtdpic._lib import lib
