@@ -298,19 +298,33 @@ def bench_sweep(args, flush):
         f_ms.append(a0.elapsed_time(a1))
         s_ms.append(a1.elapsed_time(b1))
     fields_ms, spectra_ms = statistics.median(f_ms), statistics.median(s_ms)
+    # the same spectra on the CUDA cores, for comparison
+    sw.dft = "cuda"
+    c_ms = []
+    for _ in range(2):
+        b0, b1 = _events()
+        b0.record()
+        sw.launch_spectra(st)
+        b1.record()
+        b1.synchronize()
+        c_ms.append(b0.elapsed_time(b1))
+    sw.dft = "tc"
     cells = sw.cell_steps()
     status = sw.packed.d_status.cpu().numpy()
     fallbacks = int(sw.packed.d_fallbacks.cpu().numpy().sum())
     plain_rate, plain_ms = sweep.plain_per_instance_rate(grids, max_instances=16)
     batched = cells / ((fields_ms + spectra_ms) * 1e-3)
-    dft_flops = 8.0 * 2 * sw.n * sw.S * sw.F
+    dft_flops = 2.0 * (2 * sw.n) * (2 * sw.F) * sw.S  # real GEMM [2n x S] x [S x 2F]
     return {"workload": "sweep_4096inst_nz500-8000_steps8192_kerr_f32",
             "instances": sw.n, "time_steps": sw.S, "freqs": sw.F,
             "fields_ms": round(fields_ms, 2), "spectra_ms": round(spectra_ms, 2),
             "mcell_steps_per_s": round(batched / 1e6, 1),
             "plain_mcell_steps_per_s": round(plain_rate / 1e6, 1),
             "vs_plain": round(batched / plain_rate, 1),
-            "dft_tflops": round(dft_flops / (spectra_ms * 1e-3) / 1e12, 2),
+            "dft": "tcgen05 split-BF16x3, FP32 chunk sums, FP64 across chunks",
+            "dft_gemm_tflops": round(dft_flops / (spectra_ms * 1e-3) / 1e12, 2),
+            "dft_tensor_tflops": round(3 * dft_flops / (spectra_ms * 1e-3) / 1e12, 2),
+            "dft_cuda_core_ms": round(min(c_ms), 2), "dft_tc_error": sw.dft_error(),
             "fp64_cubic_resolves": fallbacks, "bad_status": int((status != 0).sum()),
             "plain": "same resident kernel, one instance per launch, 16 instances in sequence"}
 

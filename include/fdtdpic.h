@@ -178,12 +178,16 @@ int fdtdpic_dft_probes(int precision, const void *d_traces, int R, int S, int rp
                        int64_t sp, int64_t sn, const void *d_tw, int F, double *d_out,
                        fdtdpic_stream_t stream);
 /* The same X on the tensor cores (tcgen05, sm_103a): split-BF16x3 products (about 16
- * significant bits each) with FP32 sums over 64-step chunks in tensor memory and FP64 sums
- * across chunks.  d_err (one int32, caller-zeroed) is set non-zero if a bounded wait for the
- * tensor cores gave up (the affected outputs are then not written). */
+ * significant bits each) with FP32 sums over 256-step groups in tensor memory and FP64 sums
+ * across groups.  The operands are first packed into BF16 tiles in d_scratch (16-byte aligned,
+ * fdtdpic_dft_tc_scratch_bytes(R, S, F) bytes).  d_err (one int32, caller-zeroed) is set
+ * non-zero if a bounded wait for the copies or the tensor cores gave up (the affected outputs
+ * are then not written). */
+int64_t fdtdpic_dft_tc_scratch_bytes(int R, int S, int F);
 int fdtdpic_dft_probes_tc(int precision, const void *d_traces, int R, int S, int rp, int64_t ldp,
                           int64_t sp, int64_t sn, const void *d_tw, int F, double *d_out,
-                          int32_t *d_err, fdtdpic_stream_t stream);
+                          void *d_scratch, int64_t scratch_bytes, int32_t *d_err,
+                          fdtdpic_stream_t stream);
 /* |R(f)| = |X[2p+1, f]| / |X[2p, f]| for n_pairs trace pairs (0 where |X[2p, f]| = 0). */
 int fdtdpic_reflection_ratio(const double *d_X, int n_pairs, int F, double *d_ratio,
                              fdtdpic_stream_t stream);

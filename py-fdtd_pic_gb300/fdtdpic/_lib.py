@@ -152,9 +152,11 @@ def _declare(L):
     L.fdtdpic_dft_probes.restype = c_int
     L.fdtdpic_dft_probes.argtypes = [c_int, P, c_int, c_int, c_int, c_i64, c_i64, c_i64, P,
                                      c_int, P, P]
+    L.fdtdpic_dft_tc_scratch_bytes.restype = c_i64
+    L.fdtdpic_dft_tc_scratch_bytes.argtypes = [c_int, c_int, c_int]
     L.fdtdpic_dft_probes_tc.restype = c_int
     L.fdtdpic_dft_probes_tc.argtypes = [c_int, P, c_int, c_int, c_int, c_i64, c_i64, c_i64, P,
-                                        c_int, P, P, P]
+                                        c_int, P, P, c_i64, P, P]
     L.fdtdpic_reflection_ratio.restype = c_int
     L.fdtdpic_reflection_ratio.argtypes = [P, c_int, c_int, P, P]
     L.fdtdpic_slot_layout.restype = c_int

@@ -99,9 +99,10 @@ def make_sweep_grids(spec: SweepSpec, eps0=None, mu0=None, mode=MODE_KERR):
 class Sweep:
     """A batch resident on the GPU: ``run()`` enqueues the persistent batch launch, the DFT of
     both probe traces of every instance and |R(f)|; ``capture()`` records that sequence once
-    as a CUDA graph, after which ``run()`` replays it."""
+    as a CUDA graph, after which ``run()`` replays it.  dft: "tc" (tensor cores, split-BF16x3;
+    ``dft_error()`` reports a tensor-core wait that gave up) or "cuda" (FP32 CUDA cores)."""
 
-    def __init__(self, grids, dt, freqs, precision="f32", threads=256, grid_ctas=0):
+    def __init__(self, grids, dt, freqs, precision="f32", threads=256, grid_ctas=0, dft="tc"):
         self.L = lib()
         self.grids = grids
         self.n = len(grids)
@@ -124,6 +125,13 @@ class Sweep:
                                           engine._ptr(self.d_tw), st), "fdtdpic_dft_twiddles")
         self.d_X = torch.empty(2 * self.n * self.F * 2, dtype=torch.float64, device=dev)
         self.d_R = torch.empty(self.n * self.F, dtype=torch.float64, device=dev)
+        if dft not in ("tc", "cuda"):
+            raise ValueError("dft must be 'tc' (tensor cores) or 'cuda' (CUDA cores)")
+        self.dft = dft
+        self.d_err = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.tc_bytes = int(self.L.fdtdpic_dft_tc_scratch_bytes(2 * self.n, self.S, self.F))
+        self.d_tc = (torch.empty(self.tc_bytes, dtype=torch.uint8, device=dev)
+                     if dft == "tc" else None)
         self.graph = None
 
     def _enqueue(self, stream):
@@ -138,9 +146,19 @@ class Sweep:
         """DFT of both probe traces of every instance, then |R(f)|."""
         p = self.packed
         st = ctypes.c_void_p(stream.cuda_stream)
-        check(self.L.fdtdpic_dft_probes(p.prec, engine._ptr(p.d_probe), 2 * self.n, self.S, 2,
-                                        2 * self.S, 1, 2, engine._ptr(self.d_tw), self.F,
-                                        engine._ptr(self.d_X), st), "fdtdpic_dft_probes")
+        if self.dft == "tc":
+            if self.d_tc is None:
+                self.d_tc = torch.empty(self.tc_bytes, dtype=torch.uint8, device=p.d_probe.device)
+            check(self.L.fdtdpic_dft_probes_tc(p.prec, engine._ptr(p.d_probe), 2 * self.n, self.S,
+                                               2, 2 * self.S, 1, 2, engine._ptr(self.d_tw),
+                                               self.F, engine._ptr(self.d_X),
+                                               engine._ptr(self.d_tc), self.tc_bytes,
+                                               engine._ptr(self.d_err), st),
+                  "fdtdpic_dft_probes_tc")
+        else:
+            check(self.L.fdtdpic_dft_probes(p.prec, engine._ptr(p.d_probe), 2 * self.n, self.S,
+                                            2, 2 * self.S, 1, 2, engine._ptr(self.d_tw), self.F,
+                                            engine._ptr(self.d_X), st), "fdtdpic_dft_probes")
         check(self.L.fdtdpic_reflection_ratio(engine._ptr(self.d_X), self.n, self.F,
                                               engine._ptr(self.d_R), st),
               "fdtdpic_reflection_ratio")
@@ -162,6 +180,9 @@ class Sweep:
             self.graph.replay()
         else:
             self._enqueue(stream or torch.cuda.current_stream())
+
+    def dft_error(self) -> int:
+        return int(self.d_err.item())
 
     def reflection(self):
         return self.d_R.cpu().numpy().reshape(self.n, self.F)

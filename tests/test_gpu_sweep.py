@@ -79,12 +79,17 @@ def test_dft_tensor_cores_match_numpy(precision):
     d_tw = torch.empty(int(L.fdtdpic_dft_twiddle_bytes(F, S)), dtype=torch.uint8, device="cuda")
     d_out = torch.full((2 * n_pairs * F * 2,), float("nan"), dtype=torch.float64, device="cuda")
     d_err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nb = int(L.fdtdpic_dft_tc_scratch_bytes(2 * n_pairs, S, F))
+    d_scr = torch.empty(nb, dtype=torch.uint8, device="cuda")
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     check(L.fdtdpic_dft_twiddles(engine._ptr(d_f), F, S, dt, engine._ptr(d_tw), st))
     prec = 4 if precision == "f32" else 8
+    assert L.fdtdpic_dft_probes_tc(prec, engine._ptr(d_x), 2 * n_pairs, S, 2, 2 * S, 1, 2,
+                                   engine._ptr(d_tw), F, engine._ptr(d_out), engine._ptr(d_scr),
+                                   nb - 16, engine._ptr(d_err), st) != 0  # scratch too small
     check(L.fdtdpic_dft_probes_tc(prec, engine._ptr(d_x), 2 * n_pairs, S, 2, 2 * S, 1, 2,
-                                  engine._ptr(d_tw), F, engine._ptr(d_out), engine._ptr(d_err),
-                                  st))
+                                  engine._ptr(d_tw), F, engine._ptr(d_out), engine._ptr(d_scr), nb,
+                                  engine._ptr(d_err), st))
     torch.cuda.synchronize()
     assert int(d_err.item()) == 0
     got = d_out.cpu().numpy().reshape(2 * n_pairs, F, 2)
@@ -126,16 +131,17 @@ def _oracle_probes(spec, p, src):
     return r
 
 
-@pytest.fixture(scope="module")
-def small_sweep():
+@pytest.fixture(scope="module", params=["tc", "cuda"])
+def small_sweep(request):
     _torch()
     import torch
     from fdtdpic import sweep
     spec = sweep.SweepSpec(**SMALL)
     grids, dt = sweep.make_sweep_grids(spec)
-    sw = sweep.Sweep(grids, dt, spec.freqs(), precision="f32")
+    sw = sweep.Sweep(grids, dt, spec.freqs(), precision="f32", dft=request.param)
     sw.run()
     torch.cuda.synchronize()
+    assert sw.dft_error() == 0
     return spec, grids, dt, sw
 
 
@@ -178,7 +184,7 @@ def test_sweep_graph_replay_and_alone_equal_batch(small_sweep):
     spec, grids, dt, sw = small_sweep
     base_p = sw.d_probe_view().copy()
     base_R = sw.reflection().copy()
-    sw2 = sweep.Sweep(grids, dt, spec.freqs(), precision="f32", threads=512)
+    sw2 = sweep.Sweep(grids, dt, spec.freqs(), precision="f32", threads=512, dft=sw.dft)
     sw2.capture()
     for _ in range(2):
         sw2.run()
@@ -186,7 +192,7 @@ def test_sweep_graph_replay_and_alone_equal_batch(small_sweep):
     np.testing.assert_array_equal(sw2.d_probe_view(), base_p)
     np.testing.assert_array_equal(sw2.reflection(), base_R)
     for k in (0, len(grids) - 1):
-        one = sweep.Sweep([grids[k]], dt, spec.freqs(), precision="f32")
+        one = sweep.Sweep([grids[k]], dt, spec.freqs(), precision="f32", dft=sw.dft)
         one.run()
         torch.cuda.synchronize()
         np.testing.assert_array_equal(one.d_probe_view()[0], base_p[k])
