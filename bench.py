@@ -209,11 +209,16 @@ def run_ours(args):
         push_ms = tm.push_ms / T
         achieved = BYTES_PER_PARTICLE * NP / (push_ms * 1e-3) / 1e9
     peak, peak_kind = _peaks()
+    # DRAM bytes per launch of the dominant kernel from one ncu capture of this command
+    # (profiles/<kernel>_traffic.json, written from the capture summarised beside it)
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "pic_push_kernel_traffic.json")
+    prof = os.path.join(ROOT, "profiles",
+                        ("pic_tiled_kernel" if tiled else "pic_push_kernel") + "_traffic.json")
     if os.path.exists(prof):
         try:
-            traffic = float(json.load(open(prof))["dram_bytes_per_launch"])
+            tj = json.load(open(prof))
+            if int(tj.get("time_steps", T)) == T:
+                traffic = float(tj["dram_bytes_per_launch"])
         except Exception:
             traffic = None
 

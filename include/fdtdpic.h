@@ -33,7 +33,7 @@ extern "C" {
 
 typedef struct CUstream_st *fdtdpic_stream_t; /* == cudaStream_t */
 
-#define FDTDPIC_ABI_VERSION 1
+#define FDTDPIC_ABI_VERSION 2
 
 #define FDTDPIC_OK 0
 #define FDTDPIC_ERR_ARG (-1)     /* invalid argument (sizes, pointers, modes) */
@@ -117,6 +117,9 @@ typedef struct FdtdInstance {
     int64_t probe_offset; /* elements into d_probe: [n_steps][2] */
     int64_t state_offset; /* elements into d_state: FDTD_STATE_ARRAYS x (nz+1) */
     int64_t hist_offset;  /* elements into d_hist: [hist_rows][nz+1] */
+    int64_t srcs_offset;  /* doubles into d_src: Exs[t]/sc then Hys[t]/sc (n_steps each), the
+                             source divided by courantNo ahead of time (the same correctly rounded
+                             FP64 quotients the kernels would form); -1: divide on the device */
 } FdtdInstance;
 
 /* ---- library ---------------------------------------------------------------------------- */

@@ -158,7 +158,7 @@ int fdtdpic_instance_layout(int64_t *out, int n)
         offsetof(FdtdInstance, nl_e0), offsetof(FdtdInstance, nl_e0chi),
         offsetof(FdtdInstance, pml_offset), offsetof(FdtdInstance, src_offset),
         offsetof(FdtdInstance, probe_offset), offsetof(FdtdInstance, state_offset),
-        offsetof(FdtdInstance, hist_offset)};
+        offsetof(FdtdInstance, hist_offset), offsetof(FdtdInstance, srcs_offset)};
     const int nv = (int)(sizeof(v) / sizeof(v[0]));
     for (int i = 0; i < n && i < nv; ++i) out[i] = v[i];
     return nv;

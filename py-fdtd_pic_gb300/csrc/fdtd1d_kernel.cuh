@@ -121,15 +121,32 @@ __device__ inline Scal<T> scal_block(const FdtdInstance &I)
     return s_c;
 }
 
+// Source values of step t in T, (T)(Exs[t]/Sc) and (T)(Hys[t]/Sc) (TF/SF only), from the
+// precomputed quotients when the descriptor has them (srcs_offset >= 0), else divided here.
+// pool: the source pool (the instance's offsets index it).
 template <typename T>
-__device__ inline void source_block(const FdtdInstance &I, const double *src, int t, T &src_e,
+__device__ __forceinline__ T src_e_at(const FdtdInstance &I, const double *pool, int t)
+{
+    return I.srcs_offset >= 0 ? (T)pool[I.srcs_offset + t] : (T)(pool[I.src_offset + t] / I.sc);
+}
+
+template <typename T>
+__device__ __forceinline__ T src_h_at(const FdtdInstance &I, const double *pool, int t)
+{
+    if (!I.tfsf) return T(0);
+    return I.srcs_offset >= 0 ? (T)pool[I.srcs_offset + I.n_steps + t]
+                              : (T)(pool[I.src_offset + I.n_steps + t] / I.sc);
+}
+
+template <typename T>
+__device__ inline void source_block(const FdtdInstance &I, const double *pool, int t, T &src_e,
                                     T &src_h)
 {
     __shared__ T s_v[2];
     __syncthreads();
     if (threadIdx.x == 0) {
-        s_v[0] = (T)(src[t] / I.sc);
-        s_v[1] = I.tfsf ? (T)(src[I.n_steps + t] / I.sc) : T(0);
+        s_v[0] = src_e_at<T>(I, pool, t);
+        s_v[1] = src_h_at<T>(I, pool, t);
     }
     __syncthreads();
     src_e = s_v[0];
@@ -340,8 +357,6 @@ __device__ void run_instance_resident(const BatchArgs<T> &args, const FdtdInstan
     const Scal<T> c = make_scal<T>(I);
     Kerr<T> kr;
     kr.setup(I);
-    const double *Exs = args.src + I.src_offset;
-    const double *Hys = Exs + I.n_steps;
     T *probe = args.probe + I.probe_offset;
     T *hist = args.hist ? args.hist + I.hist_offset : nullptr;
     int nfb = 0;
@@ -350,8 +365,8 @@ __device__ void run_instance_resident(const BatchArgs<T> &args, const FdtdInstan
     __shared__ T s_src[2][2];
     __syncthreads();  // a previous instance of this CTA may still read s_src
     if (tid == 0 && I.step_begin < I.step_end) {
-        s_src[I.step_begin & 1][0] = (T)(Exs[I.step_begin] / I.sc);
-        s_src[I.step_begin & 1][1] = I.tfsf ? (T)(Hys[I.step_begin] / I.sc) : T(0);
+        s_src[I.step_begin & 1][0] = src_e_at<T>(I, args.src, I.step_begin);
+        s_src[I.step_begin & 1][1] = src_h_at<T>(I, args.src, I.step_begin);
     }
     __syncthreads();
 
@@ -373,8 +388,8 @@ __device__ void run_instance_resident(const BatchArgs<T> &args, const FdtdInstan
                 for (int k = tid; k < n; k += nt) hist[(int64_t)row * n + k] = s.ex[k];
         }
         if (tid == nt - 1 && t + 1 < I.step_end) {
-            s_src[(t + 1) & 1][0] = (T)(Exs[t + 1] / I.sc);
-            s_src[(t + 1) & 1][1] = I.tfsf ? (T)(Hys[t + 1] / I.sc) : T(0);
+            s_src[(t + 1) & 1][0] = src_e_at<T>(I, args.src, t + 1);
+            s_src[(t + 1) & 1][1] = src_h_at<T>(I, args.src, t + 1);
         }
         __syncthreads();
     }
@@ -452,7 +467,7 @@ __global__ void __launch_bounds__(256, 4) fdtd_global_e_kernel(BatchArgs<T> args
     Kerr<T> kr;
     kerr_setup_block<T>(kr, I);
     T src_e, src_h;
-    source_block<T>(I, args.src + I.src_offset, t, src_e, src_h);
+    source_block<T>(I, args.src, t, src_e, src_h);
     const int n = I.nz + 1;
     T *gA = args.state + I.state_offset + (int64_t)FDTD_ST_A * n;
     int nfb = 0;
@@ -467,8 +482,7 @@ __global__ void __launch_bounds__(256, 4) fdtd_global_h_kernel(BatchArgs<T> args
     const FdtdInstance &I = instance_block(args.inst[0]);
     GlobalStore<T, true> s = global_store<T, true>(I, args);
     const Scal<T> c = scal_block<T>(I);
-    const double *Hys = args.src + I.src_offset + I.n_steps;
-    const T src_h = I.tfsf ? (T)(Hys[t] / I.sc) : T(0);
+    const T src_h = src_h_at<T>(I, args.src, t);
     const int n = I.nz + 1;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     for (int k = 1 + gt; k < n - 1; k += gridDim.x * blockDim.x) h_cell<T>(I, c, s, k, src_h);

@@ -180,24 +180,52 @@ __device__ __forceinline__ void smem_add_u64(unsigned long long *p, unsigned lon
     if (hadd) atomicAdd(w + 1, hadd);
 }
 
-// One lane's deposit words: into the CTA's shared window when the node falls in it, else
-// straight into the global accumulators.  (A warp-aggregated form -- match-any plus segmented
-// reductions per node -- measured 3x slower on GB300 than these direct shared atomics.)
+// Sum a uint64 over the 32 lanes of a full warp exactly (wrap-around two's complement): three
+// pieces of at most 22 bits through the warp reduction unit, so no piece's sum overflows 32 bits.
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
+{
+    const unsigned c0 = (unsigned)(v & 0x3FFFFFull);
+    const unsigned c1 = (unsigned)((v >> 22) & 0x3FFFFFull);
+    const unsigned c2 = (unsigned)(v >> 44);
+    const unsigned long long s0 = __reduce_add_sync(0xffffffffu, c0);
+    const unsigned long long s1 = __reduce_add_sync(0xffffffffu, c1);
+    const unsigned long long s2 = __reduce_add_sync(0xffffffffu, c2);
+    return s0 + (s1 << 22) + (s2 << 44);
+}
+
+// Add each lane's word to arr[idx] (idx < 0: nothing), all 32 lanes calling.  When the whole
+// warp targets one index -- a dense beam after re-binning puts 32 consecutive particles in one
+// cell -- the warp sums first and one lane adds; otherwise every lane adds its own word (shared
+// atomics that rarely collide at low density).
+__device__ __forceinline__ void warp_add_u64(unsigned long long *arr, int idx, unsigned long long v)
+{
+    const int i0 = __shfl_sync(0xffffffffu, idx, 0);
+    if (__all_sync(0xffffffffu, idx == i0)) {
+        if (i0 < 0) return;
+        const unsigned long long sum = warp_sum_u64(v);
+        if ((threadIdx.x & 31) == 0 && sum != 0ull) smem_add_u64(arr + i0, sum);
+    } else if (idx >= 0 && v != 0ull) {
+        smem_add_u64(arr + idx, v);
+    }
+}
+
+// One deposit slot for the whole warp (every lane calls it; invalid lanes pass node = -1):
+// nodes inside the CTA's shared window go through warp_add_u64, the rest straight into the
+// global accumulators.
 template <int W>
 __device__ __forceinline__ void deposit_slot(unsigned long long *win, unsigned long long *acc,
                                              int nz1, int base, int word0, int node,
                                              const long long *val)
 {
-    if (node < 0) return;
     const int rel = node - base;
+    const bool in_win = node >= 0 && rel >= 0 && rel < PIC_WIN;
+    const bool out = node >= 0 && !in_win;
 #pragma unroll
     for (int w = 0; w < W; ++w) {
-        const unsigned long long s = (unsigned long long)val[w];
-        if (s == 0ull) continue;
-        if (rel >= 0 && rel < PIC_WIN)
-            smem_add_u64(win + (size_t)(word0 + w) * PIC_WIN + rel, s);
-        else
-            atomicAdd(acc + (size_t)(word0 + w) * nz1 + node, s);
+        warp_add_u64(win + (size_t)(word0 + w) * PIC_WIN, in_win ? rel : -1,
+                     (unsigned long long)val[w]);
+        if (out && val[w] != 0) atomicAdd(acc + (size_t)(word0 + w) * nz1 + node,
+                                          (unsigned long long)val[w]);
     }
 }
 
@@ -385,7 +413,7 @@ __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
     Kerr<T> kr;
     consts_block<T>(a.fc, c, kr);
     T src_e, src_h;
-    source_block<T>(I, a.f.src + I.src_offset, t, src_e, src_h);
+    source_block<T>(I, a.f.src, t, src_e, src_h);
     const int n = I.nz + 1;
     T *gA = a.f.state + I.state_offset + (int64_t)FDTD_ST_A * n;
     int nfb = 0;
@@ -403,7 +431,7 @@ __global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
     Scal<T> c;
     Kerr<T> kr;
     consts_block<T>(a.fc, c, kr);
-    const T src_h = I.tfsf ? (T)(a.f.src[I.src_offset + I.n_steps + t] / I.sc) : T(0);
+    const T src_h = src_h_at<T>(I, a.f.src, t);
     const int n = I.nz + 1;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     for (int k = 1 + gt; k < n - 1; k += gridDim.x * blockDim.x) h_cell<T>(I, c, s, k, src_h);
@@ -429,7 +457,7 @@ __global__ void __launch_bounds__(1024) pic_field_fused_kernel(PicField<T> a, in
     Kerr<T> kr;
     consts_block<T>(a.fc, c, kr);
     T src_e, src_h;
-    source_block<T>(I, a.f.src + I.src_offset, t, src_e, src_h);
+    source_block<T>(I, a.f.src, t, src_e, src_h);
     const int n = I.nz + 1;
     T *gA = a.f.state + I.state_offset + (int64_t)FDTD_ST_A * n;
     int nfb = 0;

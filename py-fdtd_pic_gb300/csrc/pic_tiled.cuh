@@ -416,10 +416,9 @@ __global__ void __launch_bounds__(TILE_THREADS, 1) pic_tiled_kernel(TileArgs<T> 
         __syncthreads();
         // ---------------- E phase ----------------
         if (tid == 0) {
-            const double *Exs = a.f.src + I.src_offset;
             const bool src_here = I.nzsrc >= c0 - 1 && I.nzsrc <= c1 + 1;
-            s_src[0] = src_here ? (T)(Exs[t] / I.sc) : T(0);
-            s_src[1] = (src_here && I.tfsf) ? (T)(Exs[I.n_steps + t] / I.sc) : T(0);
+            s_src[0] = src_here ? src_e_at<T>(I, a.f.src, t) : T(0);
+            s_src[1] = src_here ? src_h_at<T>(I, a.f.src, t) : T(0);
         }
         for (int l = tid; l < L; l += nt) {
             hyp[l] = hy[l];

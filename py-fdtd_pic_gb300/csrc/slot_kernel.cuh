@@ -47,13 +47,11 @@ __device__ void run_instance_cta_global(const BatchArgs<T> &args, const FdtdInst
     T *gA = gst + (int64_t)FDTD_ST_A * n;
     if (!I.resume)
         for (int64_t i = tid; i < (int64_t)FDTD_STATE_ARRAYS * n; i += nt) gst[i] = T(0);
-    const double *Exs = args.src + I.src_offset;
-    const double *Hys = Exs + I.n_steps;
     __shared__ T s_src[2][2];
     __syncthreads();
     if (tid == 0 && I.step_begin < I.step_end) {
-        s_src[I.step_begin & 1][0] = (T)(Exs[I.step_begin] / I.sc);
-        s_src[I.step_begin & 1][1] = I.tfsf ? (T)(Hys[I.step_begin] / I.sc) : T(0);
+        s_src[I.step_begin & 1][0] = src_e_at<T>(I, args.src, I.step_begin);
+        s_src[I.step_begin & 1][1] = src_h_at<T>(I, args.src, I.step_begin);
     }
     __syncthreads();
     const Scal<T> c = make_scal<T>(I);
@@ -80,8 +78,8 @@ __device__ void run_instance_cta_global(const BatchArgs<T> &args, const FdtdInst
                 for (int k = tid; k < n; k += nt) hist[(int64_t)row * n + k] = s.Ex(k);
         }
         if (tid == nt - 1 && t + 1 < I.step_end) {
-            s_src[(t + 1) & 1][0] = (T)(Exs[t + 1] / I.sc);
-            s_src[(t + 1) & 1][1] = I.tfsf ? (T)(Hys[t + 1] / I.sc) : T(0);
+            s_src[(t + 1) & 1][0] = src_e_at<T>(I, args.src, t + 1);
+            s_src[(t + 1) & 1][1] = src_h_at<T>(I, args.src, t + 1);
         }
         __syncthreads();
     }
@@ -142,7 +140,6 @@ __device__ void run_beam_slot(FdtdSlot &S, const FdtdInstance &I, unsigned char 
     const Scal<T> c = make_scal<T>(I);
     Kerr<T> kr;
     kr.setup(I);
-    const double *Exs = fa.src + I.src_offset;
     T *probe = fa.probe + I.probe_offset;
     T *hist = fa.hist ? fa.hist + I.hist_offset : nullptr;
     __shared__ T s_src[2];
@@ -151,8 +148,8 @@ __device__ void run_beam_slot(FdtdSlot &S, const FdtdInstance &I, unsigned char 
     for (int t = I.step_begin; t < I.step_end; ++t) {
         const bool last = (t == I.step_end - 1);
         if (tid == 0) {
-            s_src[0] = (T)(Exs[t] / I.sc);
-            s_src[1] = I.tfsf ? (T)(Exs[I.n_steps + t] / I.sc) : T(0);
+            s_src[0] = src_e_at<T>(I, fa.src, t);
+            s_src[1] = src_h_at<T>(I, fa.src, t);
         }
         // push: gather E^t and B^t, Boris, move, deposit Jx^(t+1/2) (and Jz on the last step)
         for (int p = tid; p < np; p += nt) {

@@ -97,7 +97,7 @@ _I4 = [("nz", "<i4"), ("n_steps", "<i4"), ("step_begin", "<i4"), ("step_end", "<
 _F8 = [(n, "<f8") for n in ("ue", "ue_slab", "uh", "uh_slab", "dtdz", "eps0", "sc", "pol_a",
                             "pol_b", "pol_c", "kerr_a", "kerr_b", "kerr_c", "nl_e0", "nl_e0chi")]
 _I8 = [(n, "<i8") for n in ("pml_offset", "src_offset", "probe_offset", "state_offset",
-                            "hist_offset")]
+                            "hist_offset", "srcs_offset")]
 INSTANCE_DTYPE = np.dtype(_I4 + _F8 + _I8, align=True)
 INSTANCE_FIELDS = [f[0] for f in _I4 + _F8 + _I8]
 

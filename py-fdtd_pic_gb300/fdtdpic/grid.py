@@ -74,6 +74,7 @@ class Grid:
 
     def descriptor(self) -> np.ndarray:
         d = np.zeros((), INSTANCE_DTYPE)
+        d["srcs_offset"] = -1  # set by pack() with the precomputed quotients
         d["nz"], d["n_steps"] = self.nz, self.n_steps
         d["step_begin"], d["step_end"] = self.step_begin, self.step_end
         d["pml"], d["cpml_lo"], d["cpml_hi"] = self.pml, int(self.cpml_lo), int(self.cpml_hi)
@@ -237,13 +238,17 @@ def pack(grids, itemsize):
         d["pml_offset"] = off_tab
         tabs.append(g.table.ravel())
         off_tab += g.table.size
-        key = (id(g.exs), id(g.hys), g.n_steps)
+        key = (id(g.exs), id(g.hys), g.n_steps, float(g.sc))
         if key not in src_index:
             src_index[key] = off_src
-            srcs.append(np.asarray(g.exs[:g.n_steps], np.float64))
-            srcs.append(np.asarray(g.hys[:g.n_steps], np.float64))
-            off_src += 2 * g.n_steps
+            exs = np.asarray(g.exs[:g.n_steps], np.float64)
+            hys = np.asarray(g.hys[:g.n_steps], np.float64)
+            # the per-step source values Exs[t]/Sc, Hys[t]/Sc (IEEE division: the same quotients
+            # a kernel would form), so no kernel divides in FP64 on its critical path
+            srcs += [exs, hys, exs / float(g.sc), hys / float(g.sc)]
+            off_src += 4 * g.n_steps
         d["src_offset"] = src_index[key]
+        d["srcs_offset"] = src_index[key] + 2 * g.n_steps
         d["probe_offset"] = off_probe
         off_probe += 2 * g.n_steps
         d["state_offset"] = off_state

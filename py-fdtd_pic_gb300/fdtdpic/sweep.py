@@ -201,6 +201,23 @@ class Sweep:
         return float(sum((g.nz + 1) * (g.step_end - g.step_begin) for g in self.grids))
 
 
+def shard_indices(grids, rank, world):
+    """Instances of rank ``rank`` out of ``world`` when a sweep is split across GPUs: longest
+    (by predicted cost) first, each to the currently lightest rank -- the instances are
+    independent, so the ranks need no collective on the data path, only a gather of results."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("need 0 <= rank < world")
+    order = sorted(range(len(grids)), key=lambda i: (-grids[i].cost(), i))
+    load = [0.0] * world
+    mine = []
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        load[r] += grids[i].cost()
+        if r == rank:
+            mine.append(i)
+    return sorted(mine)
+
+
 def plain_per_instance_rate(grids, precision="f32", threads=256, max_instances=32):
     """Cell-steps/s of the plain form -- one instance per launch, launched one after another --
     on up to max_instances of the batch (the baseline the batched launch is compared with)."""
@@ -284,3 +301,33 @@ def autotune(grids, precision="f32", probe_steps=256, candidates=(128, 256, 512,
 def _copy_grid(g):
     from dataclasses import replace
     return replace(g)
+
+
+def _main(argv=None):
+    """One sweep of the seeded ragged batch: ``python -m fdtdpic.sweep --instances N --steps T``
+    (profiling driver; prints the field and spectra times)."""
+    import argparse
+    ap = argparse.ArgumentParser(description=_main.__doc__)
+    ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--steps", type=int, default=8192)
+    ap.add_argument("--dft", choices=["tc", "cuda"], default="tc")
+    ap.add_argument("--threads", type=int, default=256)
+    a = ap.parse_args(argv)
+    spec = SweepSpec(n_inst=a.instances, n_steps=a.steps)
+    grids, dt = make_sweep_grids(spec)
+    sw = Sweep(grids, dt, spec.freqs(), precision="f32", threads=a.threads, dft=a.dft)
+    st = torch.cuda.current_stream()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0.record()
+    sw.launch_fields(st)
+    e1.record()
+    sw.launch_spectra(st)
+    e2.record()
+    e2.synchronize()
+    print(json.dumps(dict(instances=sw.n, steps=sw.S, fields_ms=e0.elapsed_time(e1),
+                          spectra_ms=e1.elapsed_time(e2), dft=a.dft,
+                          dft_error=sw.dft_error())))
+
+
+if __name__ == "__main__":
+    _main()

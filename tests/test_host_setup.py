@@ -68,7 +68,7 @@ def test_library_loads_and_exports_header_symbols():
     assert len(names) >= 7
     for n in names:
         assert hasattr(L, n), n
-    assert L.fdtdpic_abi_version() == 1
+    assert L.fdtdpic_abi_version() == 2
     assert L.fdtdpic_strerror(-1) == b"invalid argument"
 
 
