@@ -217,7 +217,8 @@ def run_ours(args):
     if os.path.exists(prof):
         try:
             tj = json.load(open(prof))
-            if int(tj.get("time_steps", T)) == T:
+            # the tiled kernel's launch covers every step of the run; a push launch one step
+            if not tiled or int(tj.get("time_steps", T)) == T:
                 traffic = float(tj["dram_bytes_per_launch"])
         except Exception:
             traffic = None
@@ -228,8 +229,10 @@ def run_ours(args):
             dist.destroy_process_group()
         return None
     # our kernels per run: tiled = init, bin, the persistent kernel, offsets, unbin, status;
-    # streaming = push + fused field per step, 3 re-binning kernels every 32 steps, 3 others
-    launches_per_run = 6 if tiled else 2 * T + 3 * (T // 32) + 3
+    # streaming = push, E phase and H phase per step, five re-binning kernels (histogram,
+    # three-launch scan, scatter) every 32 steps, the step counter's advance per 64-step graph
+    # block, and init, constants, step-counter set and finish per run
+    launches_per_run = 6 if tiled else 3 * T + 5 * (T // 32) + T // 64 + 4
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
@@ -246,6 +249,7 @@ def run_ours(args):
                 "ms_per_step": round(e2e_ms, 3)},
         "roofline": {"bound": "hbm",
                      "kernel": "pic_tiled_kernel<float>" if tiled else "pic_push_kernel<float>",
+                     "path": "tiled" if tiled else "streaming",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 3), "peak_source": peak_kind,
                      "traffic": traffic,

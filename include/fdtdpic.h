@@ -210,7 +210,9 @@ typedef struct PicBeam {
     int32_t clo, chi;   /* periodic beam domain, cells [clo, chi); 2 <= clo < chi <= nz-2 */
     int32_t sort_every; /* re-bin by cell every this many steps (0: never) */
     int32_t chunk;      /* particles per CTA in the push kernel (0: library default) */
-    int32_t path;       /* 0: automatic, 1: streaming kernels, 2: persistent tiled kernel */
+    int32_t path;       /* 0: automatic (= streaming, measured faster on GB300 at every size
+                           but the smallest, where the two tie), 1: streaming kernels,
+                           2: persistent tiled kernel */
     double kE;     /* q dt / (2 m c) */
     double kH;     /* -q mu0 dt / (2 m) */
     double sc;     /* c dt / dz */
@@ -232,10 +234,10 @@ typedef struct FdtdPicTiming {
 
 /* Bytes of caller scratch fdtdpic_run needs (deposit accumulators, re-binning buffers). */
 int64_t fdtdpic_scratch_bytes(int precision, int nz, int n_part);
-/* Bytes of scratch with which fdtdpic_run can take the persistent tiled path for this run on the
- * current device (the streaming requirement when that path does not apply).  The tiled path
- * applies when the grid splits into at least two tiles of >= max(pml+2, 8) cells, one per SM;
- * fdtdpic_run takes it whenever beam->path allows and scratch_bytes covers it. */
+/* Bytes of scratch fdtdpic_run needs for this run on the current device: for beam->path == 2
+ * the persistent tiled path's requirement (the tiled path applies when the grid splits into at
+ * least two tiles of >= max(pml+2, 8) cells, one per SM, each fitting shared memory), else the
+ * streaming path's. */
 int64_t fdtdpic_pic_scratch_bytes(int precision, const FdtdInstance *inst, const PicBeam *beam);
 /* The largest power-of-two scale for which no deposit accumulator can overflow. */
 double fdtdpic_pic_jscale(const PicBeam *beam);

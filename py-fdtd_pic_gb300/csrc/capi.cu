@@ -49,7 +49,7 @@ static TileGeom tiled_geometry(int precision, const FdtdInstance &h, const PicBe
 {
     TileGeom g{};
     int dev = 0, sms = 0, max_optin = 0;
-    if (b.path == 1 || cudaGetDevice(&dev) != cudaSuccess ||
+    if (b.path != 2 || cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
             cudaSuccess)

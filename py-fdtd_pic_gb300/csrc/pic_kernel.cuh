@@ -19,6 +19,31 @@ namespace fdtdpic {
 
 int cuda_status(cudaError_t e);
 
+// Programmatic dependent launch: the push and field kernels of consecutive steps are launched
+// with programmatic stream serialization, each lets the next one launch as soon as all its own
+// CTAs run (pdl_trigger), and each waits for its predecessor's completion and memory (pdl_wait)
+// only after the set-up that does not read it (shared-memory copies of the constants, clearing
+// the deposit window).  Steps then pay no launch gap and overlap those prologues.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), int grid, int block, cudaStream_t st,
+                              Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 constexpr int PIC_WIN = 256;      // shared-memory deposit window (nodes) per CTA
 constexpr int PIC_THREADS = 256;  // push kernel CTA size
 
@@ -235,11 +260,13 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
     constexpr int W = Fix<T>::W;
     __shared__ unsigned long long win[2 * W * PIC_WIN];
     __shared__ int base_s;
+    pdl_trigger();
     const int b0 = blockIdx.x * a.chunk;
     const int b1 = min(a.n_part, b0 + a.chunk);
     if (b0 >= b1) return;
     const int nz1 = a.nz + 1;
     for (int i = threadIdx.x; i < 2 * W * PIC_WIN; i += blockDim.x) win[i] = 0ull;
+    pdl_wait();  // the previous step's fields and particles
     if (threadIdx.x == 0) base_s = a.cell[b0] - 8;
     __syncthreads();
     const int base = base_s;
@@ -347,14 +374,15 @@ struct PicField {
     T *jx, *jz, *hyp;
     double jinv;
     float jinv_f;
-    const int32_t *step;  // device step counter (graph replay); NULL: use the launch argument
+    const int32_t *step;  // graph replay: first step of the replayed block (the launch argument
+                          // is the offset within it); NULL: the launch argument is the step
     int last;             // the call's last step: Jz was deposited, Jz and Acubic are written out
 };
 
 template <typename T>
 __device__ __forceinline__ int pic_step_index(const PicField<T> &a, int t)
 {
-    return a.step ? *a.step : t;
+    return a.step ? *a.step + t : t;
 }
 
 // E phase of cell k with the beam: Hyp <- Hy (H^(t+1/2) for the next push), currents out of the
@@ -406,12 +434,14 @@ __device__ __forceinline__ void pic_probes(PicField<T> &a, const FdtdInstance &I
 template <typename T>
 __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
 {
+    pdl_trigger();
     const FdtdInstance &I = instance_block(a.f.inst[0]);
-    const int t = pic_step_index(a, t_arg);
     GlobalStore<T, true> s = global_store<T, true>(I, a.f);
     Scal<T> c;
     Kerr<T> kr;
     consts_block<T>(a.fc, c, kr);
+    pdl_wait();  // the push's deposits (and, through it, the step counter)
+    const int t = pic_step_index(a, t_arg);
     T src_e, src_h;
     source_block<T>(I, a.f.src, t, src_e, src_h);
     const int n = I.nz + 1;
@@ -425,12 +455,14 @@ __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
 template <typename T>
 __global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
 {
+    pdl_trigger();
     const FdtdInstance &I = instance_block(a.f.inst[0]);
-    const int t = pic_step_index(a, t_arg);
     GlobalStore<T, true> s = global_store<T, true>(I, a.f);
     Scal<T> c;
     Kerr<T> kr;
     consts_block<T>(a.fc, c, kr);
+    pdl_wait();  // the E phase
+    const int t = pic_step_index(a, t_arg);
     const T src_h = src_h_at<T>(I, a.f.src, t);
     const int n = I.nz + 1;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -439,16 +471,16 @@ __global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
     pic_probes<T>(a, I, s, t, gt, gridDim.x * blockDim.x, n);
 }
 
-// Advances the device step counter after a multi-CTA field step.
-static __global__ void pic_tick_kernel(int32_t *step) { *step += 1; }
+// The device step counter: set before the first replayed block, advanced by a block's length
+// at the end of each block (one launch per block, not per step).
+static __global__ void pic_advance_kernel(int32_t *step, int k) { *step += k; }
 static __global__ void pic_set_step_kernel(int32_t *step, int t) { *step = t; }
 
 // Whole field step in one CTA (grids up to PIC_FUSED_MAX cells): E phase, barrier, H phase,
-// probes, then the step counter moves on.  Saves two launches per step.
-constexpr int PIC_FUSED_MAX = 32768;
+// probes.  Saves a launch per step.
+constexpr int PIC_FUSED_MAX = 1024;
 template <typename T>
-__global__ void __launch_bounds__(1024) pic_field_fused_kernel(PicField<T> a, int32_t *step_w,
-                                                                int t_arg)
+__global__ void __launch_bounds__(1024) pic_field_fused_kernel(PicField<T> a, int t_arg)
 {
     const FdtdInstance &I = instance_block(a.f.inst[0]);
     const int t = pic_step_index(a, t_arg);
@@ -468,16 +500,25 @@ __global__ void __launch_bounds__(1024) pic_field_fused_kernel(PicField<T> a, in
     if (threadIdx.x == 0) tfsf_edge<T>(I, s, src_h);
     pic_probes<T>(a, I, s, t, threadIdx.x, blockDim.x, n);
     if (nfb && a.f.fallbacks) atomicAdd(a.f.fallbacks, nfb);
-    __syncthreads();
-    if (threadIdx.x == 0 && step_w) *step_w = t + 1;
 }
 
 // ---- re-binning by cell (counting sort; order within a cell is not kept and does not matter)
+// The particles are in cell order from the last re-binning (and have moved little since), so
+// at high density a whole warp often holds one cell: it then takes one atomic of 32 instead of
+// 32 colliding ones.  Otherwise each lane counts its own particle.
 static __global__ void pic_hist_kernel(int n_part, const int32_t *cell, int32_t *counts, int nz1)
 {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_part; p += gridDim.x * blockDim.x) {
-        const int c = cell[p];
-        if (c >= 0 && c < nz1) atomicAdd(counts + c, 1);
+        const int c0 = cell[p];
+        const int c = (c0 >= 0 && c0 < nz1) ? c0 : -1;
+        const unsigned act = __activemask();
+        const int lead = __ffs(act) - 1;
+        const int cl = __shfl_sync(act, c, lead);
+        if (__all_sync(act, c == cl)) {
+            if ((threadIdx.x & 31) == lead && cl >= 0) atomicAdd(counts + cl, __popc(act));
+        } else if (c >= 0) {
+            atomicAdd(counts + c, 1);
+        }
     }
 }
 
@@ -573,8 +614,22 @@ __global__ void pic_scatter_kernel(int n_part, const int32_t *cell, const T *fra
                                    int32_t *cell2, T *frac2, T *ux2, T *uz2, int32_t *id2)
 {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_part; p += gridDim.x * blockDim.x) {
-        const int c = cell[p];
-        const int q = (c >= 0 && c < nz1) ? atomicAdd(cursor + c, 1) : -1;
+        const int c0 = cell[p];
+        const int c = (c0 >= 0 && c0 < nz1) ? c0 : -1;
+        // a warp that holds one cell claims its slots with one atomic (see pic_hist_kernel)
+        const unsigned act = __activemask();
+        const int lane = threadIdx.x & 31;
+        const int lead = __ffs(act) - 1;
+        const int cl = __shfl_sync(act, c, lead);
+        int q;
+        if (__all_sync(act, c == cl)) {
+            int base = 0;
+            if (lane == lead && cl >= 0) base = atomicAdd(cursor + cl, __popc(act));
+            base = __shfl_sync(act, base, lead);
+            q = (cl >= 0) ? base + __popc(act & ((1u << lane) - 1u)) : -1;
+        } else {
+            q = (c >= 0) ? atomicAdd(cursor + c, 1) : -1;
+        }
         if (q < 0 || q >= n_part) continue;
         cell2[q] = c;
         frac2[q] = frac[p];
@@ -687,7 +742,7 @@ void pic_enqueue_step(PicPlan<T> &P, const PicBeam &bm, int t, bool do_sort, boo
     if (bm.n_part > 0) {
         if (tm) tm->begin(&tm->out->push_ms);
         P.pa.deposit_jz = last_step ? 1 : 0;
-        pic_push_kernel<T><<<P.pblocks, PIC_THREADS, 0, st>>>(P.pa);
+        launch_pdl(pic_push_kernel<T>, P.pblocks, PIC_THREADS, st, P.pa);
         if (tm) tm->end();
     }
     PicField<T> pf = P.pf;
@@ -695,11 +750,10 @@ void pic_enqueue_step(PicPlan<T> &P, const PicBeam &bm, int t, bool do_sort, boo
     pf.last = last_step ? 1 : 0;
     if (tm) tm->begin(&tm->out->field_ms);
     if (P.fused) {
-        pic_field_fused_kernel<T><<<1, 1024, 0, st>>>(pf, device_step ? P.step : nullptr, t);
+        pic_field_fused_kernel<T><<<1, 1024, 0, st>>>(pf, t);
     } else {
-        pic_e_kernel<T><<<P.fblocks, P.threads, 0, st>>>(pf, t);
-        pic_h_kernel<T><<<P.fblocks, P.threads, 0, st>>>(pf, t);
-        if (device_step) pic_tick_kernel<<<1, 1, 0, st>>>(P.step);
+        launch_pdl(pic_e_kernel<T>, P.fblocks, P.threads, st, pf, t);
+        launch_pdl(pic_h_kernel<T>, P.fblocks, P.threads, st, pf, t);
     }
     if (tm) tm->end();
 }
@@ -807,8 +861,9 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
             if (e != cudaSuccess) return cuda_status(e);
             bool cb = false;
             for (int j = 0; j < K; ++j)
-                pic_enqueue_step<T>(P, bm, 0, sorting && (j % bm.sort_every) == 0, cb, true, cs,
+                pic_enqueue_step<T>(P, bm, j, sorting && (j % bm.sort_every) == 0, cb, true, cs,
                                     nullptr, false);
+            pic_advance_kernel<<<1, 1, 0, cs>>>(P.step, K);
             cudaGraph_t graph = nullptr;
             e = cudaStreamEndCapture(cs, &graph);
             if (e != cudaSuccess) return cuda_status(e);

@@ -78,8 +78,9 @@ def beam_constants(dz, dt, weight, mu0, q=Q_E, m=M_E):
 class PicRun:
     """One grid plus a beam, resident on the GPU; ``step(n)`` advances n steps.
 
-    path: "auto" (the persistent tiled kernel when the grid can be tiled over the SMs, else the
-    streaming kernels), "streaming" or "tiled"."""
+    path: "auto" (the streaming kernels: push, field and re-binning launches captured in CUDA
+    graphs; measured faster than the persistent tiled kernel on GB300), "streaming" or "tiled"
+    (one cooperative launch for all steps; grids that tile over the SMs only)."""
 
     def __init__(self, grid: Grid, beam: Beam, dz: float, dt: float, mu0: float,
                  precision="f32", sort_every=32, chunk=0, path="auto", device=None):
