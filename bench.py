@@ -358,17 +358,10 @@ def bench_large(args, flush):
     """One large instance: Nz = 2^24 cells, 64M macroparticles over the whole grid, Kerr slab
     over the middle half, FP32, streaming PIC path; timed over --large-steps of its 20,000 steps
     after a 64-step warm-up (the rate per step is the same over the run)."""
-    import scipy.constants as sc
     import torch
-    from fdtdpic.grid import lorentz_kerr_grid
-    from fdtdpic.pic import FdtdPicTiming, PicRun, make_beam
+    from fdtdpic.pic import FdtdPicTiming, large_case
     nz, npart, total = 1 << 24, 64 << 20, 20000
-    g = lorentz_kerr_grid(nz, total, front=nz // 4, rear=3 * nz // 4, nzsrc=NZSRC,
-                          probes=(50, nz - 50), chi3=1e-2)
-    beam = make_beam(npart, 50, nz - 51, DZ, seed=7, sort=False)
-    dt = 0.5 * DZ / 299792458.0
-    run = PicRun(g, beam, DZ, dt, sc.mu_0, precision="f32", sort_every=32)
-    del beam
+    run = large_case(nz, npart, total, dz=DZ, nzsrc=NZSRC)
     run.step(64)
     torch.cuda.synchronize()
     n = args.large_steps

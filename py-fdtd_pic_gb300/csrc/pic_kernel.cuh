@@ -218,17 +218,26 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
     return s0 + (s1 << 22) + (s2 << 44);
 }
 
-// Add each lane's word to arr[idx] (idx < 0: nothing), all 32 lanes calling.  When the whole
-// warp targets one index -- a dense beam after re-binning puts 32 consecutive particles in one
-// cell -- the warp sums first and one lane adds; otherwise every lane adds its own word (shared
-// atomics that rarely collide at low density).
+// Add each lane's word to arr[idx] (idx < 0: nothing), all 32 lanes calling.  The particles
+// are in cell order, so a warp's nodes form a few runs of equal values (a dense beam: one or two):
+// with at most three runs the warp sums the words of each distinct node and one lane adds the
+// sum; otherwise every lane adds its own word (shared atomics that rarely collide at low
+// density).  Integer sums: the result does not depend on which way a warp takes.
 __device__ __forceinline__ void warp_add_u64(unsigned long long *arr, int idx, unsigned long long v)
 {
-    const int i0 = __shfl_sync(0xffffffffu, idx, 0);
-    if (__all_sync(0xffffffffu, idx == i0)) {
-        if (i0 < 0) return;
-        const unsigned long long sum = warp_sum_u64(v);
-        if ((threadIdx.x & 31) == 0 && sum != 0ull) smem_add_u64(arr + i0, sum);
+    const int lane = threadIdx.x & 31;
+    const int prev = __shfl_up_sync(0xffffffffu, idx, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || idx != prev);
+    if (__popc(heads) <= 3) {
+        unsigned todo = __ballot_sync(0xffffffffu, idx >= 0);
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            const int node = __shfl_sync(0xffffffffu, idx, src);
+            const bool mine = idx == node;
+            const unsigned long long sum = warp_sum_u64(mine ? v : 0ull);
+            if (lane == src && sum != 0ull) smem_add_u64(arr + node, sum);
+            todo &= ~__ballot_sync(0xffffffffu, mine);
+        }
     } else if (idx >= 0 && v != 0ull) {
         smem_add_u64(arr + idx, v);
     }
@@ -316,8 +325,15 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
             a.ux[p] = uxn;
             a.uz[p] = uzn;
         }
-        deposit_slot<W>(win, a.acc, nz1, base, 0, nx0, vx0);
-        deposit_slot<W>(win, a.acc, nz1, base, 0, nx1, vx1);
+        // a warp whose Jx words are all zero (particles no field has given transverse momentum)
+        // skips both Jx slots: adding zeros changes nothing
+        long long jx_any = 0;
+#pragma unroll
+        for (int w = 0; w < W; ++w) jx_any |= vx0[w] | vx1[w];
+        if (__any_sync(0xffffffffu, jx_any != 0)) {
+            deposit_slot<W>(win, a.acc, nz1, base, 0, nx0, vx0);
+            deposit_slot<W>(win, a.acc, nz1, base, 0, nx1, vx1);
+        }
         if (a.deposit_jz) {
             deposit_slot<W>(win, a.acc, nz1, base, W, nzA, vzA);
             deposit_slot<W>(win, a.acc, nz1, base, W, nzB, vzB);
@@ -503,22 +519,34 @@ __global__ void __launch_bounds__(1024) pic_field_fused_kernel(PicField<T> a, in
 }
 
 // ---- re-binning by cell (counting sort; order within a cell is not kept and does not matter)
-// The particles are in cell order from the last re-binning (and have moved little since), so
-// at high density a whole warp often holds one cell: it then takes one atomic of 32 instead of
-// 32 colliding ones.  Otherwise each lane counts its own particle.
+// The particles are in cell order from the last re-binning (and have moved little since), so a
+// warp's 32 particles form a few runs of equal cells: each run takes one atomic for all its
+// lanes (run heads: lanes whose cell differs from the previous lane's).  The loops run whole
+// warps (out-of-range lanes carry cell -1).
+
+// Lanes of the run that lane `lane` heads (heads: the warp's run-head mask, lane a head).
+__device__ __forceinline__ int run_length(unsigned heads, int lane)
+{
+    const unsigned later = heads & ~((2u << lane) - 1u);  // heads after this lane (none: 0)
+    return (later ? __ffs(later) - 1 : 32) - lane;
+}
+// The head of the run holding lane `lane`.
+__device__ __forceinline__ int run_head(unsigned heads, int lane)
+{
+    return 31 - __clz(heads & ((2u << lane) - 1u));
+}
+
 static __global__ void pic_hist_kernel(int n_part, const int32_t *cell, int32_t *counts, int nz1)
 {
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_part; p += gridDim.x * blockDim.x) {
-        const int c0 = cell[p];
+    const int lane = threadIdx.x & 31;
+    for (int p0 = blockIdx.x * blockDim.x; p0 < n_part; p0 += gridDim.x * blockDim.x) {
+        const int p = p0 + threadIdx.x;
+        const int c0 = p < n_part ? cell[p] : -1;
         const int c = (c0 >= 0 && c0 < nz1) ? c0 : -1;
-        const unsigned act = __activemask();
-        const int lead = __ffs(act) - 1;
-        const int cl = __shfl_sync(act, c, lead);
-        if (__all_sync(act, c == cl)) {
-            if ((threadIdx.x & 31) == lead && cl >= 0) atomicAdd(counts + cl, __popc(act));
-        } else if (c >= 0) {
-            atomicAdd(counts + c, 1);
-        }
+        const int prev = __shfl_up_sync(0xffffffffu, c, 1);
+        const bool head = lane == 0 || c != prev;
+        const unsigned heads = __ballot_sync(0xffffffffu, head);
+        if (head && c >= 0) atomicAdd(counts + c, run_length(heads, lane));
     }
 }
 
@@ -613,29 +641,29 @@ __global__ void pic_scatter_kernel(int n_part, const int32_t *cell, const T *fra
                                    const T *uz, const int32_t *id, int32_t *cursor, int nz1,
                                    int32_t *cell2, T *frac2, T *ux2, T *uz2, int32_t *id2)
 {
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_part; p += gridDim.x * blockDim.x) {
-        const int c0 = cell[p];
+    const int lane = threadIdx.x & 31;
+    for (int p0 = blockIdx.x * blockDim.x; p0 < n_part; p0 += gridDim.x * blockDim.x) {
+        const int p = p0 + threadIdx.x;
+        const bool in = p < n_part;
+        const int c0 = in ? cell[p] : -1;
         const int c = (c0 >= 0 && c0 < nz1) ? c0 : -1;
-        // a warp that holds one cell claims its slots with one atomic (see pic_hist_kernel)
-        const unsigned act = __activemask();
-        const int lane = threadIdx.x & 31;
-        const int lead = __ffs(act) - 1;
-        const int cl = __shfl_sync(act, c, lead);
-        int q;
-        if (__all_sync(act, c == cl)) {
-            int base = 0;
-            if (lane == lead && cl >= 0) base = atomicAdd(cursor + cl, __popc(act));
-            base = __shfl_sync(act, base, lead);
-            q = (cl >= 0) ? base + __popc(act & ((1u << lane) - 1u)) : -1;
-        } else {
-            q = (c >= 0) ? atomicAdd(cursor + c, 1) : -1;
-        }
-        if (q < 0 || q >= n_part) continue;
+        T f = T(0), x = T(0), z = T(0);
+        int i = 0;
+        if (c >= 0) { f = frac[p]; x = ux[p]; z = uz[p]; i = id[p]; }
+        // each run of equal cells claims its slots with one atomic (see pic_hist_kernel)
+        const int prev = __shfl_up_sync(0xffffffffu, c, 1);
+        const bool head = lane == 0 || c != prev;
+        const unsigned heads = __ballot_sync(0xffffffffu, head);
+        int base = 0;
+        if (head && c >= 0) base = atomicAdd(cursor + c, run_length(heads, lane));
+        const int h = run_head(heads, lane);
+        const int q = __shfl_sync(0xffffffffu, base, h) + (lane - h);
+        if (c < 0 || q >= n_part) continue;
         cell2[q] = c;
-        frac2[q] = frac[p];
-        ux2[q] = ux[p];
-        uz2[q] = uz[p];
-        id2[q] = id[p];
+        frac2[q] = f;
+        ux2[q] = x;
+        uz2[q] = z;
+        id2[q] = i;
     }
 }
 

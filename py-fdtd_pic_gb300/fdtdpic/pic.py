@@ -175,3 +175,56 @@ class PicRun:
 
     def status(self):
         return self.d_status.cpu().numpy()
+
+
+def large_case(nz=1 << 24, n_part=64 << 20, total=20000, dz=0.015, nzsrc=100, precision="f32",
+               sort_every=32, path="auto"):
+    """The large single-instance workload: ``nz`` cells, ``n_part`` macroparticles spread over
+    the whole grid, a Kerr slab over the middle half, ``total`` steps (at the default sizes:
+    2^24 cells, 64M particles, 20,000 steps, FP32)."""
+    import scipy.constants as sc
+
+    from .grid import lorentz_kerr_grid
+    g = lorentz_kerr_grid(nz, total, front=nz // 4, rear=3 * nz // 4, nzsrc=nzsrc,
+                          probes=(50, nz - 50), chi3=1e-2)
+    beam = make_beam(n_part, 50, nz - 51, dz, seed=7, sort=False)
+    return PicRun(g, beam, dz, 0.5 * dz / C0, sc.mu_0, precision=precision,
+                  sort_every=sort_every, path=path)
+
+
+def _main(argv=None):
+    """``python -m fdtdpic.pic --nz N --particles P --steps S``: the large-instance workload at
+    the given sizes; prints milliseconds per step (CUDA events) and the per-kernel split."""
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(prog="python -m fdtdpic.pic")
+    ap.add_argument("--nz", type=int, default=1 << 24)
+    ap.add_argument("--particles", type=int, default=64 << 20)
+    ap.add_argument("--steps", type=int, default=256)
+    ap.add_argument("--warmup", type=int, default=64)
+    ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
+    ap.add_argument("--path", choices=["auto", "streaming", "tiled"], default="auto")
+    a = ap.parse_args(argv)
+    run = large_case(a.nz, a.particles, a.warmup + 2 * a.steps, precision=a.precision,
+                     path=a.path)
+    run.step(a.warmup)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    run.step(a.steps)
+    e1.record()
+    e1.synchronize()
+    tm = FdtdPicTiming()
+    run.step(a.steps, timing=tm)
+    ms = e0.elapsed_time(e1) / a.steps
+    print(json.dumps({"nz": a.nz, "n_part": a.particles, "steps": a.steps,
+                      "ms_per_step": round(ms, 4),
+                      "kernel_ms_per_step": {"push": round(tm.push_ms / a.steps, 4),
+                                             "field": round(tm.field_ms / a.steps, 4),
+                                             "sort": round(tm.sort_ms / a.steps, 4)},
+                      "status": [int(x) for x in run.status()]}))
+
+
+if __name__ == "__main__":
+    _main()

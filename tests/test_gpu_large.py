@@ -14,14 +14,8 @@ def _run(steps):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
-    import scipy.constants as sc
-    from fdtdpic.grid import lorentz_kerr_grid
-    from fdtdpic.pic import PicRun, make_beam
-    nz, npart = 1 << 24, 64 << 20
-    g = lorentz_kerr_grid(nz, 20000, front=nz // 4, rear=3 * nz // 4, nzsrc=100,
-                          probes=(50, nz - 50), chi3=1e-2)
-    beam = make_beam(npart, 50, nz - 51, DZ, seed=7, sort=False)
-    run = PicRun(g, beam, DZ, 0.5 * DZ / 299792458.0, sc.mu_0, precision="f32")
+    from fdtdpic.pic import large_case
+    run = large_case(1 << 24, 64 << 20, 20000, dz=DZ, nzsrc=100)
     run.step(steps)
     torch.cuda.synchronize()
     return run
