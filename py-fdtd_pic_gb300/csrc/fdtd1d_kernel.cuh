@@ -192,6 +192,53 @@ struct GlobalStore {
     __device__ T tab_at(int row, int col) const { return (T)tab[row * W + col]; }
 };
 
+// One cell's state in registers, for the grid-stride field kernels: a thread issues the loads
+// of several cells (FIELD_UE in the E phase, FIELD_U in the H phase) before it updates any of
+// them (the loads are in flight together), then runs
+// e_cell / h_cell on the register copies and stores what the update changed.  The same e_cell /
+// h_cell arithmetic as the global-memory store.
+constexpr int FIELD_U = 4;   // H phase
+constexpr int FIELD_UE = 2;  // E phase (the Kerr solve holds more registers)
+template <typename T>
+struct RegE {
+    T ex, hk, hkm, dx, p, pp, psi;
+    const double *tab;
+    int k, W;
+    __device__ T &Ex(int) { return ex; }
+    __device__ T HyR(int kk) const { return kk == k ? hk : hkm; }
+    __device__ T &Dx(int) { return dx; }
+    __device__ T &P(int) { return p; }
+    __device__ T &Pp(int) { return pp; }
+    __device__ T &PsiE(int, int) { return psi; }
+    __device__ T tab_at(int row, int col) const { return (T)tab[row * W + col]; }
+};
+template <typename T>
+struct RegH {
+    T hy, exk, exk1, psi;
+    const double *tab;
+    int k, W;
+    __device__ T &Hy(int) { return hy; }
+    __device__ T ExR(int kk) const { return kk == k ? exk : exk1; }
+    __device__ T &PsiH(int, int) { return psi; }
+    __device__ T tab_at(int row, int col) const { return (T)tab[row * W + col]; }
+};
+// Which state cell k's updates touch besides Ex and Hy (e_cell / h_cell's conditions).
+struct CellUse {
+    bool dx, p, pp_w, psie, psih;
+};
+__device__ __forceinline__ CellUse cell_use(const FdtdInstance &I, int k)
+{
+    const int n = I.nz + 1;
+    const bool slab = k >= I.front && k < I.rear;
+    CellUse u;
+    u.dx = slab && I.mode != FDTD_MODE_FREESPACE;
+    u.p = slab && I.mode == FDTD_MODE_LINLOR;       // P read (both passes), P_prev too
+    u.pp_w = u.p && I.pol_active;                    // P and P_prev written
+    u.psie = (I.cpml_lo && k < I.pml) || (I.cpml_hi && k >= n - I.pml);
+    u.psih = (I.cpml_lo && k < I.pml) || (I.cpml_hi && k >= n - I.pml && k < n - 1);
+    return u;
+}
+
 // E phase for cell k in [1, nz].  src_e = Exs[t]/Sc, src_h = Hys[t]/Sc in T.
 // has_jx/jxv: the beam's grid current at cell k, entering the Ex update as the reference's -Jx
 // term and, with the beam on, the slab's Dx update too (dx_jx).
@@ -458,6 +505,55 @@ __device__ inline GlobalStore<T, NC> global_store(const FdtdInstance &I, const B
     return s;
 }
 
+// Register copies of cell k (k < kend) for e_cell / h_cell, and the stores of what they changed.
+template <typename T>
+__device__ __forceinline__ void e_cell_load(const FdtdInstance &I, const GlobalStore<T, true> &s,
+                                            int k, int kend, RegE<T> &r)
+{
+    r.tab = s.tab;
+    r.W = s.W;
+    r.k = k;
+    const bool in = k < kend;
+    const CellUse u = cell_use(I, k);
+    r.hk = in ? __ldg(s.hy + k) : T(0);
+    r.hkm = (in && k >= 1) ? __ldg(s.hy + k - 1) : T(0);
+    r.ex = in ? s.ex[k] : T(0);
+    r.dx = (in && u.dx) ? s.dx[k] : T(0);
+    r.p = (in && u.p) ? s.p[k] : T(0);
+    r.pp = (in && u.p) ? s.pp[k] : T(0);
+    r.psi = (in && u.psie) ? s.psie[k] : T(0);
+}
+template <typename T>
+__device__ __forceinline__ void e_cell_store(const FdtdInstance &I, GlobalStore<T, true> &s, int k,
+                                             const RegE<T> &r)
+{
+    const CellUse u = cell_use(I, k);
+    s.ex[k] = r.ex;
+    if (u.dx) s.dx[k] = r.dx;
+    if (u.pp_w) { s.p[k] = r.p; s.pp[k] = r.pp; }
+    if (u.psie) s.psie[k] = r.psi;
+}
+template <typename T>
+__device__ __forceinline__ void h_cell_load(const FdtdInstance &I, const GlobalStore<T, true> &s,
+                                            int k, int kend, RegH<T> &r)
+{
+    r.tab = s.tab;
+    r.W = s.W;
+    r.k = k;
+    const bool in = k < kend;
+    r.hy = in ? s.hy[k] : T(0);
+    r.exk = in ? __ldg(s.ex + k) : T(0);
+    r.exk1 = in ? __ldg(s.ex + k + 1) : T(0);
+    r.psi = (in && cell_use(I, k).psih) ? s.psih[k] : T(0);
+}
+template <typename T>
+__device__ __forceinline__ void h_cell_store(const FdtdInstance &I, GlobalStore<T, true> &s, int k,
+                                             const RegH<T> &r)
+{
+    s.hy[k] = r.hy;
+    if (cell_use(I, k).psih) s.psih[k] = r.psi;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256, 4) fdtd_global_e_kernel(BatchArgs<T> args, int t)
 {
@@ -470,9 +566,20 @@ __global__ void __launch_bounds__(256, 4) fdtd_global_e_kernel(BatchArgs<T> args
     source_block<T>(I, args.src, t, src_e, src_h);
     const int n = I.nz + 1;
     T *gA = args.state + I.state_offset + (int64_t)FDTD_ST_A * n;
+    const int stride = gridDim.x * blockDim.x;
     int nfb = 0;
-    for (int k = 1 + blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-        e_cell<T>(I, c, kr, s, k, src_e, src_h, false, T(0), gA, &nfb);
+    for (int k0 = 1 + blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += FIELD_UE * stride) {
+        RegE<T> r[FIELD_UE];
+#pragma unroll
+        for (int u = 0; u < FIELD_UE; ++u) e_cell_load<T>(I, s, k0 + u * stride, n, r[u]);
+#pragma unroll
+        for (int u = 0; u < FIELD_UE; ++u) {
+            const int k = k0 + u * stride;
+            if (k >= n) break;
+            e_cell<T>(I, c, kr, r[u], k, src_e, src_h, false, T(0), gA, &nfb);
+            e_cell_store<T>(I, s, k, r[u]);
+        }
+    }
     if (nfb && args.fallbacks) atomicAdd(args.fallbacks, nfb);
 }
 
@@ -485,7 +592,19 @@ __global__ void __launch_bounds__(256, 4) fdtd_global_h_kernel(BatchArgs<T> args
     const T src_h = src_h_at<T>(I, args.src, t);
     const int n = I.nz + 1;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    for (int k = 1 + gt; k < n - 1; k += gridDim.x * blockDim.x) h_cell<T>(I, c, s, k, src_h);
+    const int stride = gridDim.x * blockDim.x;
+    for (int k0 = 1 + gt; k0 < n - 1; k0 += FIELD_U * stride) {
+        RegH<T> r[FIELD_U];
+#pragma unroll
+        for (int u = 0; u < FIELD_U; ++u) h_cell_load<T>(I, s, k0 + u * stride, n - 1, r[u]);
+#pragma unroll
+        for (int u = 0; u < FIELD_U; ++u) {
+            const int k = k0 + u * stride;
+            if (k >= n - 1) break;
+            h_cell<T>(I, c, r[u], k, src_h);
+            h_cell_store<T>(I, s, k, r[u]);
+        }
+    }
     if (gt == 0) tfsf_edge<T>(I, s, src_h);
 }
 

@@ -226,6 +226,13 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 __device__ __forceinline__ void warp_add_u64(unsigned long long *arr, int idx, unsigned long long v)
 {
     const int lane = threadIdx.x & 31;
+    const int i0 = __shfl_sync(0xffffffffu, idx, 0);
+    if (__all_sync(0xffffffffu, idx == i0)) {  // one node for the whole warp
+        if (i0 < 0) return;
+        const unsigned long long sum = warp_sum_u64(v);
+        if (lane == 0 && sum != 0ull) smem_add_u64(arr + i0, sum);
+        return;
+    }
     const int prev = __shfl_up_sync(0xffffffffu, idx, 1);
     const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || idx != prev);
     if (__popc(heads) <= 3) {
@@ -281,17 +288,25 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
     const int base = base_s;
     const int Lc = a.chi - a.clo;
     const int iters = (b1 - b0 + blockDim.x - 1) / blockDim.x;
+    const int lane = threadIdx.x & 31;
     int lost = 0;
+    // this thread's next particle, loaded one iteration ahead so its loads overlap the current
+    // particle's gathers and push
+    int nc = 0;
+    T nf = T(0), nux = T(0), nuz = T(0);
+    if (b0 + (int)threadIdx.x < b1) {
+        const int p = b0 + threadIdx.x;
+        nc = a.cell[p]; nf = a.frac[p]; nux = a.ux[p]; nuz = a.uz[p];
+    }
     for (int it = 0; it < iters; ++it) {
         const int p = b0 + it * blockDim.x + threadIdx.x;
         bool valid = p < b1;
-        int c = 0;
-        T f = T(0);
-        if (valid) {
-            c = a.cell[p];
-            f = a.frac[p];
-            if (c < 1 || c + 2 > a.nz) { valid = false; ++lost; }
-        }
+        int c = nc;
+        T f = nf;
+        const T ux0 = nux, uz0 = nuz;
+        const int pn = p + blockDim.x;
+        if (pn < b1) { nc = a.cell[pn]; nf = a.frac[pn]; nux = a.ux[pn]; nuz = a.uz[pn]; }
+        if (valid && (c < 1 || c + 2 > a.nz)) { valid = false; ++lost; }
         int nx0 = -1, nx1 = -1, nzA = -1, nzB = -1;
         long long vx0[W], vx1[W], vzA[W], vzB[W];
 #pragma unroll
@@ -305,7 +320,7 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
             const T H = (T(1) - fh) * (T(0.5) * (__ldg(a.hy + j) + __ldg(a.hyp + j))) +
                         fh * (T(0.5) * (__ldg(a.hy + j + 1) + __ldg(a.hyp + j + 1)));
             Moved<T> m;
-            particle_step<T>(E, H, c, f, a.ux[p], a.uz[p], a.kE, a.kH, a.sc, a.kJ, a.kJz, m);
+            particle_step<T>(E, H, c, f, ux0, uz0, a.kE, a.kH, a.sc, a.kJ, a.kJz, m);
             const T uxn = m.ux, uzn = m.uz, f1 = m.f1;
             int c1 = m.c1;
             nx0 = m.nx0;
@@ -331,8 +346,23 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
 #pragma unroll
         for (int w = 0; w < W; ++w) jx_any |= vx0[w] | vx1[w];
         if (__any_sync(0xffffffffu, jx_any != 0)) {
-            deposit_slot<W>(win, a.acc, nz1, base, 0, nx0, vx0);
-            deposit_slot<W>(win, a.acc, nz1, base, 0, nx1, vx1);
+            // the whole warp on one node pair (a dense beam after re-binning): two warp sums
+            const int i0 = __shfl_sync(0xffffffffu, nx0, 0);
+            const int r0 = i0 - base;
+            if (__all_sync(0xffffffffu, nx0 == i0) && i0 >= 0 && r0 >= 0 && r0 + 1 < PIC_WIN) {
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    const unsigned long long s0 = warp_sum_u64((unsigned long long)vx0[w]);
+                    const unsigned long long s1 = warp_sum_u64((unsigned long long)vx1[w]);
+                    if (lane == 0) {
+                        if (s0 != 0ull) smem_add_u64(win + (size_t)w * PIC_WIN + r0, s0);
+                        if (s1 != 0ull) smem_add_u64(win + (size_t)w * PIC_WIN + r0 + 1, s1);
+                    }
+                }
+            } else {
+                deposit_slot<W>(win, a.acc, nz1, base, 0, nx0, vx0);
+                deposit_slot<W>(win, a.acc, nz1, base, 0, nx1, vx1);
+            }
         }
         if (a.deposit_jz) {
             deposit_slot<W>(win, a.acc, nz1, base, W, nzA, vzA);
@@ -450,6 +480,7 @@ __device__ __forceinline__ void pic_probes(PicField<T> &a, const FdtdInstance &I
 template <typename T>
 __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
 {
+    constexpr int W = Fix<T>::W;
     pdl_trigger();
     const FdtdInstance &I = instance_block(a.f.inst[0]);
     GlobalStore<T, true> s = global_store<T, true>(I, a.f);
@@ -462,9 +493,45 @@ __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
     source_block<T>(I, a.f.src, t, src_e, src_h);
     const int n = I.nz + 1;
     T *gA = a.f.state + I.state_offset + (int64_t)FDTD_ST_A * n;
+    const int stride = gridDim.x * blockDim.x;
     int nfb = 0;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-        pic_e_cell<T>(a, I, s, c, kr, k, n, src_e, src_h, gA, &nfb);
+    // FIELD_UE cells per thread per pass, their loads (accumulator words, Hy, Ex, Dx) issued before
+    // any of them is updated; then per cell: Hyp <- Hy, accumulators cleared, the E phase with -Jx
+    for (int k0 = blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += FIELD_UE * stride) {
+        unsigned long long wx[FIELD_UE][W];
+        RegE<T> r[FIELD_UE];
+#pragma unroll
+        for (int u = 0; u < FIELD_UE; ++u) {
+            const int k = k0 + u * stride;
+#pragma unroll
+            for (int w = 0; w < W; ++w) wx[u][w] = k < n ? a.acc[(size_t)w * n + k] : 0ull;
+            e_cell_load<T>(I, s, k, n, r[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < FIELD_UE; ++u) {
+            const int k = k0 + u * stride;
+            if (k >= n) break;
+            const T jxk = Fix<T>::join(wx[u], a.jinv, a.jinv_f);
+            if (k >= 1) {
+                e_cell<T>(I, c, kr, r[u], k, src_e, src_h, true, jxk, a.last ? gA : nullptr, &nfb,
+                          true);
+                e_cell_store<T>(I, s, k, r[u]);
+            }
+            a.hyp[k] = r[u].hk;
+#pragma unroll
+            for (int w = 0; w < W; ++w) a.acc[(size_t)w * n + k] = 0ull;
+            if (a.last) {  // Jz words are only deposited on the call's last step
+                unsigned long long wz[W];
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    wz[w] = a.acc[(size_t)(W + w) * n + k];
+                    a.acc[(size_t)(W + w) * n + k] = 0ull;
+                }
+                a.jx[k] = jxk;
+                a.jz[k] = Fix<T>::join(wz, a.jinv, a.jinv_f);
+            }
+        }
+    }
     if (nfb && a.f.fallbacks) atomicAdd(a.f.fallbacks, nfb);
 }
 
@@ -482,9 +549,21 @@ __global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
     const T src_h = src_h_at<T>(I, a.f.src, t);
     const int n = I.nz + 1;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    for (int k = 1 + gt; k < n - 1; k += gridDim.x * blockDim.x) h_cell<T>(I, c, s, k, src_h);
+    const int stride = gridDim.x * blockDim.x;
+    for (int k0 = 1 + gt; k0 < n - 1; k0 += FIELD_U * stride) {
+        RegH<T> r[FIELD_U];
+#pragma unroll
+        for (int u = 0; u < FIELD_U; ++u) h_cell_load<T>(I, s, k0 + u * stride, n - 1, r[u]);
+#pragma unroll
+        for (int u = 0; u < FIELD_U; ++u) {
+            const int k = k0 + u * stride;
+            if (k >= n - 1) break;
+            h_cell<T>(I, c, r[u], k, src_h);
+            h_cell_store<T>(I, s, k, r[u]);
+        }
+    }
     if (gt == 0) tfsf_edge<T>(I, s, src_h);
-    pic_probes<T>(a, I, s, t, gt, gridDim.x * blockDim.x, n);
+    pic_probes<T>(a, I, s, t, gt, stride, n);
 }
 
 // The device step counter: set before the first replayed block, advanced by a block's length
