@@ -283,21 +283,21 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
     const int nz1 = a.nz + 1;
     for (int i = threadIdx.x; i < 2 * W * PIC_WIN; i += blockDim.x) win[i] = 0ull;
     pdl_wait();  // the previous step's fields and particles
-    if (threadIdx.x == 0) base_s = a.cell[b0] - 8;
-    __syncthreads();
-    const int base = base_s;
-    const int Lc = a.chi - a.clo;
-    const int iters = (b1 - b0 + blockDim.x - 1) / blockDim.x;
-    const int lane = threadIdx.x & 31;
-    int lost = 0;
     // this thread's next particle, loaded one iteration ahead so its loads overlap the current
-    // particle's gathers and push
+    // particle's gathers and push; thread 0's first particle (b0) also places the deposit window
     int nc = 0;
     T nf = T(0), nux = T(0), nuz = T(0);
     if (b0 + (int)threadIdx.x < b1) {
         const int p = b0 + threadIdx.x;
         nc = a.cell[p]; nf = a.frac[p]; nux = a.ux[p]; nuz = a.uz[p];
     }
+    if (threadIdx.x == 0) base_s = nc - 8;
+    __syncthreads();
+    const int base = base_s;
+    const int Lc = a.chi - a.clo;
+    const int iters = (b1 - b0 + blockDim.x - 1) / blockDim.x;
+    const int lane = threadIdx.x & 31;
+    int lost = 0;
     for (int it = 0; it < iters; ++it) {
         const int p = b0 + it * blockDim.x + threadIdx.x;
         bool valid = p < b1;
@@ -308,9 +308,10 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
         if (pn < b1) { nc = a.cell[pn]; nf = a.frac[pn]; nux = a.ux[pn]; nuz = a.uz[pn]; }
         if (valid && (c < 1 || c + 2 > a.nz)) { valid = false; ++lost; }
         int nx0 = -1, nx1 = -1, nzA = -1, nzB = -1;
-        long long vx0[W], vx1[W], vzA[W], vzB[W];
+        T jx0 = T(0), jx1 = T(0);
+        long long vzA[W], vzB[W];
 #pragma unroll
-        for (int w = 0; w < W; ++w) vx0[w] = vx1[w] = vzA[w] = vzB[w] = 0;
+        for (int w = 0; w < W; ++w) vzA[w] = vzB[w] = 0;
         if (valid) {
             int j;
             T fh;
@@ -325,8 +326,8 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
             int c1 = m.c1;
             nx0 = m.nx0;
             nx1 = m.nx0 + 1;
-            Fix<T>::split(m.jx0, a.jscale, a.jscale_f, vx0);
-            Fix<T>::split(m.jx1, a.jscale, a.jscale_f, vx1);
+            jx0 = m.jx0;
+            jx1 = m.jx1;
             nzA = m.nzA;
             nzB = m.nzB;
             if (a.deposit_jz) {
@@ -340,12 +341,16 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
             a.ux[p] = uxn;
             a.uz[p] = uzn;
         }
-        // a warp whose Jx words are all zero (particles no field has given transverse momentum)
+        // a warp whose Jx values are all zero (particles no field has given transverse momentum)
         // skips both Jx slots: adding zeros changes nothing
-        long long jx_any = 0;
+        if (__any_sync(0xffffffffu, jx0 != T(0) || jx1 != T(0))) {
+            long long vx0[W], vx1[W];
 #pragma unroll
-        for (int w = 0; w < W; ++w) jx_any |= vx0[w] | vx1[w];
-        if (__any_sync(0xffffffffu, jx_any != 0)) {
+            for (int w = 0; w < W; ++w) vx0[w] = vx1[w] = 0;
+            if (nx0 >= 0) {
+                Fix<T>::split(jx0, a.jscale, a.jscale_f, vx0);
+                Fix<T>::split(jx1, a.jscale, a.jscale_f, vx1);
+            }
             // the whole warp on one node pair (a dense beam after re-binning): two warp sums
             const int i0 = __shfl_sync(0xffffffffu, nx0, 0);
             const int r0 = i0 - base;
@@ -487,10 +492,12 @@ __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
     Scal<T> c;
     Kerr<T> kr;
     consts_block<T>(a.fc, c, kr);
-    pdl_wait();  // the push's deposits (and, through it, the step counter)
+    // the step counter is only written between graph blocks, by launches that completed before
+    // this block's first kernel started; the source pool is constant
     const int t = pic_step_index(a, t_arg);
     T src_e, src_h;
     source_block<T>(I, a.f.src, t, src_e, src_h);
+    pdl_wait();  // the push's deposits
     const int n = I.nz + 1;
     T *gA = a.f.state + I.state_offset + (int64_t)FDTD_ST_A * n;
     const int stride = gridDim.x * blockDim.x;
@@ -544,9 +551,9 @@ __global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
     Scal<T> c;
     Kerr<T> kr;
     consts_block<T>(a.fc, c, kr);
-    pdl_wait();  // the E phase
     const int t = pic_step_index(a, t_arg);
     const T src_h = src_h_at<T>(I, a.f.src, t);
+    pdl_wait();  // the E phase
     const int n = I.nz + 1;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int stride = gridDim.x * blockDim.x;
