@@ -261,7 +261,8 @@ def run_ours(args):
         "gpu_launches": launches_per_run * args.steps,
         "clocks": clk.summary(),
     }
-    for name, fn in (("sweep", bench_sweep), ("serve", bench_serve), ("large", bench_large)):
+    for name, fn in (("sweep", bench_sweep), ("serve", bench_serve), ("knee", bench_serve_knee),
+                     ("large", bench_large)):
         if name in args.extra:
             try:
                 out[name] = fn(args, flush)
@@ -352,6 +353,40 @@ def bench_serve(args, flush):
     st.update(workload="serve_poisson2000_nz256-65536_steps1k-50k_np0-2M_f32",
               offered=len(reqs), offered_rps=round(len(reqs) / secs, 1))
     return {k: (round(v, 3) if isinstance(v, float) else v) for k, v in st.items()}
+
+
+def bench_serve_knee(args, flush):
+    """Saturation knee of the server: the served request stream (as in the serve section)
+    offered open-loop at each of --knee-rates for --knee-seconds; after the arrival window the
+    server drains, so every offered request is completed and counted.  Per rate: throughput over
+    the whole run, p50/p99 latency of all requests, GPU busy fraction.  The knee is the highest
+    offered rate whose p99 latency stays within twice that of the lowest rate."""
+    from fdtdpic import server
+    secs = args.knee_seconds
+    rows = []
+    for rate in [float(r) for r in args.knee_rates.split(",") if r]:
+        reqs = server.make_request_stream(rate=rate, duration=secs)
+        srv = server.Server(precision="f32", hbm_budget=150e9)
+        try:
+            t0 = srv.clock()
+            srv.run_stream(reqs, secs)
+            srv.drain()
+            elapsed = srv.clock() - t0
+            st = srv.stats(elapsed, submitted=len(reqs))
+        finally:
+            srv.close()
+        rows.append({"offered_rps": rate, "submitted": len(reqs), "completed": st["completed"],
+                     "throughput_rps": round(st["throughput_rps"], 2),
+                     "p50_s": None if st["p50_s"] is None else round(st["p50_s"], 3),
+                     "p99_s": None if st["p99_s"] is None else round(st["p99_s"], 3),
+                     "gpu_busy": round(st["gpu_busy_s"] / elapsed, 3) if elapsed > 0 else None,
+                     "elapsed_s": round(elapsed, 2)})
+    base = next((r["p99_s"] for r in rows if r["p99_s"] is not None), None)
+    knee = max((r["offered_rps"] for r in rows
+                if base is not None and r["p99_s"] is not None and r["p99_s"] <= 2 * base),
+               default=None)
+    return {"workload": "serve_nz256-65536_steps1k-50k_np0-2M_f32", "window_s": secs,
+            "rates": rows, "knee_rps": knee}
 
 
 def bench_large(args, flush):
@@ -476,9 +511,12 @@ def main():
     ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--extra", default="sweep,serve,large",
-                    help="comma-separated extra sections: sweep, serve, large ('' for none)")
+    ap.add_argument("--extra", default="sweep,serve,knee,large",
+                    help="comma-separated extra sections: sweep, serve, knee, large ('' for none)")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--knee-rates", default="4,8,16,24,32",
+                    help="offered request rates (per second) of the serving knee section")
+    ap.add_argument("--knee-seconds", type=float, default=8.0)
     ap.add_argument("--large-steps", type=int, default=256)
     ap.add_argument("--time-steps", type=int, default=None,
                     help="shorter runs for profiling under ncu (the line is then not a bench "

@@ -239,6 +239,19 @@ __device__ __forceinline__ CellUse cell_use(const FdtdInstance &I, int k)
     return u;
 }
 
+// Interior cells -- outside the PML columns of the table (pml < k < nz + 1 - pml) and not the
+// source cells nzsrc - 1, nzsrc -- have den = 1 and none of the PML, source or TF/SF terms, so
+// their E and H updates reduce to a few operations (the same operations, in the same order, as
+// e_cell / h_cell: the factor den = 1 is exact).  CELL_KERR: a Kerr slab cell; CELL_VACUUM: outside
+// the slab; CELL_GENERIC: anything else (e_cell / h_cell).
+enum { CELL_GENERIC = 0, CELL_VACUUM = 1, CELL_KERR = 2 };
+__device__ __forceinline__ int cell_kind(const FdtdInstance &I, int k)
+{
+    if (k <= I.pml || k >= I.nz + 1 - I.pml || k == I.nzsrc || k == I.nzsrc - 1) return CELL_GENERIC;
+    if (k < I.front || k >= I.rear) return CELL_VACUUM;
+    return I.mode == FDTD_MODE_KERR ? CELL_KERR : CELL_GENERIC;
+}
+
 // E phase for cell k in [1, nz].  src_e = Exs[t]/Sc, src_h = Hys[t]/Sc in T.
 // has_jx/jxv: the beam's grid current at cell k, entering the Ex update as the reference's -Jx
 // term and, with the beam on, the slab's Dx update too (dx_jx).

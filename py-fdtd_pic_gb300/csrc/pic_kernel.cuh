@@ -131,13 +131,37 @@ struct Moved {
     T f1, ux, uz; // new fraction and momenta
     int nx0;      // Jx nodes nx0, nx0+1 (CIC at the half-step midpoint)
     T jx0, jx1;
-    int nzA, nzB; // Jz half nodes (nzB < 0 when the particle stays in its cell)
+};
+
+// Jz of one particle's move (only the call's last step deposits it): half nodes nzA, nzB (nzB < 0
+// when the particle stays in its cell) and their values, from the start (c, f) and the move.
+template <typename T>
+struct MovedJz {
+    int nzA, nzB;
     T jzA, jzB;
 };
+template <typename T>
+__device__ __forceinline__ MovedJz<T> particle_jz(int c, T f, const Moved<T> &m, T kJz)
+{
+    MovedJz<T> z;
+    const int c1 = m.c1;
+    const T f1 = m.f1;
+    if (c1 == c) {
+        z.nzA = c; z.jzA = kJz * (f1 - f);
+        z.nzB = -1; z.jzB = T(0);
+    } else if (c1 == c + 1) {
+        z.nzA = c; z.jzA = kJz * (T(1) - f);
+        z.nzB = c + 1; z.jzB = kJz * f1;
+    } else {
+        z.nzA = c - 1; z.jzA = -kJz * (T(1) - f1);
+        z.nzB = c; z.jzB = -kJz * f;
+    }
+    return z;
+}
 
 template <typename T>
 __device__ __forceinline__ void particle_step(T E, T H, int c, T f, T ux, T uz, T kE, T kH, T sc,
-                                              T kJ, T kJz, Moved<T> &m)
+                                              T kJ, Moved<T> &m)
 {
     const T uxm = (sizeof(T) == 8) ? ux + kE * E : (T)fmaf((float)kE, (float)E, (float)ux);
     const T uzm = uz;
@@ -177,16 +201,6 @@ __device__ __forceinline__ void particle_step(T E, T H, int c, T f, T ux, T uz, 
     T f1 = f + dz;
     int c1 = c;
     if (f1 >= T(1)) { c1 += 1; f1 -= T(1); } else if (f1 < T(0)) { c1 -= 1; f1 += T(1); }
-    if (c1 == c) {
-        m.nzA = c; m.jzA = kJz * (f1 - f);
-        m.nzB = -1; m.jzB = T(0);
-    } else if (c1 == c + 1) {
-        m.nzA = c; m.jzA = kJz * (T(1) - f);
-        m.nzB = c + 1; m.jzB = kJz * f1;
-    } else {
-        m.nzA = c - 1; m.jzA = -kJz * (T(1) - f1);
-        m.nzB = c; m.jzB = -kJz * f;
-    }
     m.c1 = c1;
     m.f1 = f1;
     m.ux = uxn;
@@ -216,6 +230,15 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
     const unsigned long long s1 = __reduce_add_sync(0xffffffffu, c1);
     const unsigned long long s2 = __reduce_add_sync(0xffffffffu, c2);
     return s0 + (s1 << 22) + (s2 << 44);
+}
+
+// Exact sum of an int32 over the 32 lanes of a full warp: the 16-bit halves through the
+// reduction unit (each sum fits 32 bits), joined in 64 bits.
+__device__ __forceinline__ unsigned long long warp_sum_i32(int v)
+{
+    const int hi = __reduce_add_sync(0xffffffffu, v >> 16);
+    const unsigned lo = __reduce_add_sync(0xffffffffu, (unsigned)(v & 0xffff));
+    return (unsigned long long)((long long)hi * 65536 + (long long)lo);
 }
 
 // Add each lane's word to arr[idx] (idx < 0: nothing), all 32 lanes calling.  The particles
@@ -321,18 +344,19 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
             const T H = (T(1) - fh) * (T(0.5) * (__ldg(a.hy + j) + __ldg(a.hyp + j))) +
                         fh * (T(0.5) * (__ldg(a.hy + j + 1) + __ldg(a.hyp + j + 1)));
             Moved<T> m;
-            particle_step<T>(E, H, c, f, ux0, uz0, a.kE, a.kH, a.sc, a.kJ, a.kJz, m);
+            particle_step<T>(E, H, c, f, ux0, uz0, a.kE, a.kH, a.sc, a.kJ, m);
             const T uxn = m.ux, uzn = m.uz, f1 = m.f1;
             int c1 = m.c1;
             nx0 = m.nx0;
             nx1 = m.nx0 + 1;
             jx0 = m.jx0;
             jx1 = m.jx1;
-            nzA = m.nzA;
-            nzB = m.nzB;
             if (a.deposit_jz) {
-                Fix<T>::split(m.jzA, a.jscale, a.jscale_f, vzA);
-                if (nzB >= 0) Fix<T>::split(m.jzB, a.jscale, a.jscale_f, vzB);
+                const MovedJz<T> z = particle_jz<T>(c, f, m, a.kJz);
+                nzA = z.nzA;
+                nzB = z.nzB;
+                Fix<T>::split(z.jzA, a.jscale, a.jscale_f, vzA);
+                if (nzB >= 0) Fix<T>::split(z.jzB, a.jscale, a.jscale_f, vzB);
             }
             if (c1 >= a.chi) c1 -= Lc;
             else if (c1 < a.clo) c1 += Lc;
@@ -355,10 +379,18 @@ __global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
             const int i0 = __shfl_sync(0xffffffffu, nx0, 0);
             const int r0 = i0 - base;
             if (__all_sync(0xffffffffu, nx0 == i0) && i0 >= 0 && r0 >= 0 && r0 + 1 < PIC_WIN) {
+                // words that fit 32 bits (small currents) take the two-reduction sum
+                bool fit = true;
+#pragma unroll
+                for (int w = 0; w < W; ++w)
+                    fit = fit && vx0[w] == (long long)(int)vx0[w] && vx1[w] == (long long)(int)vx1[w];
+                const bool fit_all = __all_sync(0xffffffffu, fit);
 #pragma unroll
                 for (int w = 0; w < W; ++w) {
-                    const unsigned long long s0 = warp_sum_u64((unsigned long long)vx0[w]);
-                    const unsigned long long s1 = warp_sum_u64((unsigned long long)vx1[w]);
+                    const unsigned long long s0 = fit_all ? warp_sum_i32((int)vx0[w])
+                                                          : warp_sum_u64((unsigned long long)vx0[w]);
+                    const unsigned long long s1 = fit_all ? warp_sum_i32((int)vx1[w])
+                                                          : warp_sum_u64((unsigned long long)vx1[w]);
                     if (lane == 0) {
                         if (s0 != 0ull) smem_add_u64(win + (size_t)w * PIC_WIN + r0, s0);
                         if (s1 != 0ull) smem_add_u64(win + (size_t)w * PIC_WIN + r0 + 1, s1);
@@ -507,19 +539,38 @@ __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
     for (int k0 = blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += FIELD_UE * stride) {
         unsigned long long wx[FIELD_UE][W];
         RegE<T> r[FIELD_UE];
+        int kind[FIELD_UE];
 #pragma unroll
         for (int u = 0; u < FIELD_UE; ++u) {
             const int k = k0 + u * stride;
+            kind[u] = (k >= 1 && k < n) ? cell_kind(I, k) : CELL_GENERIC;
 #pragma unroll
             for (int w = 0; w < W; ++w) wx[u][w] = k < n ? a.acc[(size_t)w * n + k] : 0ull;
-            e_cell_load<T>(I, s, k, n, r[u]);
+            if (kind[u] == CELL_GENERIC) {
+                e_cell_load<T>(I, s, k, n, r[u]);
+            } else {
+                r[u].hk = __ldg(s.hy + k);
+                r[u].hkm = __ldg(s.hy + k - 1);
+                r[u].ex = s.ex[k];
+                r[u].dx = kind[u] == CELL_KERR ? s.dx[k] : T(0);
+            }
         }
 #pragma unroll
         for (int u = 0; u < FIELD_UE; ++u) {
             const int k = k0 + u * stride;
             if (k >= n) break;
             const T jxk = Fix<T>::join(wx[u], a.jinv, a.jinv_f);
-            if (k >= 1) {
+            if (kind[u] == CELL_VACUUM) {
+                // e_cell: ex + ((hk - hkm) - jx) * ue * den, den = 1
+                s.ex[k] = r[u].ex + ((r[u].hk - r[u].hkm) - jxk) * c.ue;
+            } else if (kind[u] == CELL_KERR) {
+                // e_cell's slab branch: Dx + ((hk - hkm) - jx) * dtdz * den, the Kerr root, Ex
+                const T dx = r[u].dx + ((r[u].hk - r[u].hkm) - jxk) * c.dtdz;
+                const T A = kr.root(dx, c.eps0, &nfb);
+                if (a.last) gA[k] = A;
+                s.dx[k] = dx;
+                s.ex[k] = dx / (c.e0r + c.e0chi * A);
+            } else if (k >= 1) {
                 e_cell<T>(I, c, kr, r[u], k, src_e, src_h, true, jxk, a.last ? gA : nullptr, &nfb,
                           true);
                 e_cell_store<T>(I, s, k, r[u]);
@@ -565,8 +616,15 @@ __global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
         for (int u = 0; u < FIELD_U; ++u) {
             const int k = k0 + u * stride;
             if (k >= n - 1) break;
-            h_cell<T>(I, c, r[u], k, src_h);
-            h_cell_store<T>(I, s, k, r[u]);
+            const int kd = cell_kind(I, k);
+            if (kd != CELL_GENERIC) {
+                // h_cell: hy + (ex[k+1] - ex[k]) * uh * den with den = 1 (interior cells are
+                // outside the slab or in a Kerr slab, so uh is the outside value)
+                s.hy[k] = r[u].hy + (r[u].exk1 - r[u].exk) * c.uh;
+            } else {
+                h_cell<T>(I, c, r[u], k, src_h);
+                h_cell_store<T>(I, s, k, r[u]);
+            }
         }
     }
     if (gt == 0) tfsf_edge<T>(I, s, src_h);

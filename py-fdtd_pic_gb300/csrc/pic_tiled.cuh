@@ -273,8 +273,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 1) pic_tiled_kernel(TileArgs<T> 
                 const T E = (T(1) - f) * ex[c - base] + f * ex[c + 1 - base];
                 const T H = (T(1) - fh) * (T(0.5) * (hy[j - base] + hyp[j - base])) +
                             fh * (T(0.5) * (hy[j + 1 - base] + hyp[j + 1 - base]));
-                particle_step<T>(E, H, c, f, uxU[u], uzU[u], a.kE, a.kH, a.sc, a.kJ,
-                                 a.kJz, m);
+                particle_step<T>(E, H, c, f, uxU[u], uzU[u], a.kE, a.kH, a.sc, a.kJ, m);
                 long long v[W];
                 Fix<T>::split(m.jx0, a.jscale, a.jscale_f, v);
 #pragma unroll
@@ -283,14 +282,15 @@ __global__ void __launch_bounds__(TILE_THREADS, 1) pic_tiled_kernel(TileArgs<T> 
 #pragma unroll
                 for (int w = 0; w < W; ++w) smem_add_u64(myjw + (size_t)w * L + (m.nx0 + 1 - base), (unsigned long long)v[w]);
                 if (last) {  // Jz (a diagnostic) only on the call's last step
-                Fix<T>::split(m.jzA, a.jscale, a.jscale_f, v);
+                    const MovedJz<T> z = particle_jz<T>(c, f, m, a.kJz);
+                    Fix<T>::split(z.jzA, a.jscale, a.jscale_f, v);
 #pragma unroll
-                for (int w = 0; w < W; ++w) smem_add_u64(myjw + (size_t)(W + w) * L + (m.nzA - base), (unsigned long long)v[w]);
-                }
-                if (last && m.nzB >= 0) {
-                    Fix<T>::split(m.jzB, a.jscale, a.jscale_f, v);
+                    for (int w = 0; w < W; ++w) smem_add_u64(myjw + (size_t)(W + w) * L + (z.nzA - base), (unsigned long long)v[w]);
+                    if (z.nzB >= 0) {
+                        Fix<T>::split(z.jzB, a.jscale, a.jscale_f, v);
 #pragma unroll
-                    for (int w = 0; w < W; ++w) smem_add_u64(myjw + (size_t)(W + w) * L + (m.nzB - base), (unsigned long long)v[w]);
+                        for (int w = 0; w < W; ++w) smem_add_u64(myjw + (size_t)(W + w) * L + (z.nzB - base), (unsigned long long)v[w]);
+                    }
                 }
                 cn = m.c1;
                 if (cn >= a.chi) cn -= Lc;

@@ -163,18 +163,19 @@ __device__ void run_beam_slot(FdtdSlot &S, const FdtdInstance &I, unsigned char 
             const T H = (T(1) - fh) * (T(0.5) * (s.Hy(j) + hyp[j])) +
                         fh * (T(0.5) * (s.Hy(j + 1) + hyp[j + 1]));
             Moved<T> m;
-            particle_step<T>(E, H, cp, f, ux[p], uz[p], kE, kH, scb, kJ, kJz, m);
+            particle_step<T>(E, H, cp, f, ux[p], uz[p], kE, kH, scb, kJ, m);
             long long v[W];
             Fix<T>::split(m.jx0, jscale, jscale_f, v);
             slot_deposit<W>(acc, acc_shared, n, 0, m.nx0, v);
             Fix<T>::split(m.jx1, jscale, jscale_f, v);
             slot_deposit<W>(acc, acc_shared, n, 0, m.nx0 + 1, v);
             if (last) {
-                Fix<T>::split(m.jzA, jscale, jscale_f, v);
-                slot_deposit<W>(acc, acc_shared, n, W, m.nzA, v);
-                if (m.nzB >= 0) {
-                    Fix<T>::split(m.jzB, jscale, jscale_f, v);
-                    slot_deposit<W>(acc, acc_shared, n, W, m.nzB, v);
+                const MovedJz<T> z = particle_jz<T>(cp, f, m, kJz);
+                Fix<T>::split(z.jzA, jscale, jscale_f, v);
+                slot_deposit<W>(acc, acc_shared, n, W, z.nzA, v);
+                if (z.nzB >= 0) {
+                    Fix<T>::split(z.jzB, jscale, jscale_f, v);
+                    slot_deposit<W>(acc, acc_shared, n, W, z.nzB, v);
                 }
             }
             int c1 = m.c1;
