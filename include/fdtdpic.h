@@ -312,6 +312,39 @@ typedef struct FdtdSlotItem {
     int32_t first; /* 1: t0 starts the request (zero fields, zero beam history) */
 } FdtdSlotItem;
 
+/* ---- set-up on the device -------------------------------------------------------------------
+ * The per-grid set-up of the reference, for a whole ragged batch in one launch: the CPML
+ * profile and coefficient arrays of boundCondManager (Solver_Engine.py:70-87: CPML_ScalingCalc,
+ * CPML_Ex_RC_Define, CPML_HY_RC_Define, CPML_Ex_Update_Coef, CPML_Hy_Update_Coef and
+ * denominators, BaseFDTD11.py:223-357) as the instance's PML table; UpExMat/UpHyMat
+ * (EmptySpaceCalc / Material + UpdateCoef, BaseFDTD11.py:124-132); the Kerr cubic's
+ * coefficients (Nonlin_Eqn_Setup / AcubicFinder, :795-820) and the Lorentz ADE's A, B, C
+ * (ADE_TempPolCurr, :487-538).  The plasma frequency comes in already corrected by
+ * genericStability.spatialStab (genericStability.py:12-62). */
+typedef struct FdtdSetup {
+    double dz, dt;        /* Params.dz, Params.delT */
+    double courant;       /* Params.courantNo (the float32 value) */
+    double eps0, mu0;     /* permit_0, permea_0 */
+    double char_imp;      /* Params.CharImp */
+    double eps_re, mu_re; /* slab epsRe, muRe (free-space integrator) */
+    double kappa_max, sigma_opt, alpha_max, r_scale, r_a_scale; /* CPML_Params */
+    double plasma_freq;   /* Variables.plasmaFreqE after spatialStab */
+    double omega0, gamma; /* omega_0E, gammaE */
+    double chi3, alpha3;  /* chi3Stat, alpha3 */
+    double freq_in;       /* Params.freq_in */
+    int32_t free_space;   /* 1: the slab takes UpExMat/epsRe, UpHyMat/muRe */
+    int32_t reserved;
+} FdtdSetup;
+
+/* For each instance i: reads its geometry (nz, pml, cpml_lo, cpml_hi, pml_offset) from
+ * d_inst[i], writes its coefficient fields (ue, ue_slab, uh, uh_slab, dtdz, eps0, sc, pol_a..c,
+ * kerr_a..c, nl_e0, nl_e0chi) and its FDTD_TAB_ROWS x (2 pml + 1) table at
+ * d_pml_tab + pml_offset.  All arrays in device memory; asynchronous on the stream. */
+int fdtdpic_setup_batch(int n_inst, const FdtdSetup *d_setup, FdtdInstance *d_inst,
+                        double *d_pml_tab, fdtdpic_stream_t stream);
+/* Like fdtdpic_instance_layout, for FdtdSetup. */
+int fdtdpic_setup_layout(int64_t *out, int n);
+
 /* Like fdtdpic_instance_layout, for FdtdSlot. */
 int fdtdpic_slot_layout(int64_t *out, int n);
 /* Host-side check of one slot descriptor before it is admitted (FDTDPIC_OK or ERR_ARG). */

@@ -31,6 +31,7 @@ UNITS = {
     "dft_tc.cu": [],
     "slot.cu": ["-fmad=false"],  # beam requests round as fdtdpic_run's step
     "noalloc.cu": [],
+    "setup.cu": ["-fmad=false"],  # set-up products and sums round one by one, as numpy's
 }
 
 
@@ -101,6 +102,13 @@ _I8 = [(n, "<i8") for n in ("pml_offset", "src_offset", "probe_offset", "state_o
 INSTANCE_DTYPE = np.dtype(_I4 + _F8 + _I8, align=True)
 INSTANCE_FIELDS = [f[0] for f in _I4 + _F8 + _I8]
 
+# FdtdSetup (include/fdtdpic.h): the per-grid inputs of fdtdpic_setup_batch
+SETUP_FIELDS = ["dz", "dt", "courant", "eps0", "mu0", "char_imp", "eps_re", "mu_re", "kappa_max",
+                "sigma_opt", "alpha_max", "r_scale", "r_a_scale", "plasma_freq", "omega0",
+                "gamma", "chi3", "alpha3", "freq_in"]
+SETUP_DTYPE = np.dtype([(n, "<f8") for n in SETUP_FIELDS] + [("free_space", "<i4"),
+                                                            ("reserved", "<i4")], align=True)
+
 MODE_FREESPACE, MODE_LINLOR, MODE_KERR = 0, 1, 2
 F64, F32 = 8, 4
 TAB_ROWS = 8
@@ -161,6 +169,10 @@ def _declare(L):
     L.fdtdpic_reflection_ratio.argtypes = [P, c_int, c_int, P, P]
     L.fdtdpic_slot_layout.restype = c_int
     L.fdtdpic_slot_layout.argtypes = [P, c_int]
+    L.fdtdpic_setup_layout.restype = c_int
+    L.fdtdpic_setup_layout.argtypes = [P, c_int]
+    L.fdtdpic_setup_batch.restype = c_int
+    L.fdtdpic_setup_batch.argtypes = [c_int, P, P, P, P]
     L.fdtdpic_slot_check.restype = c_int
     L.fdtdpic_slot_check.argtypes = [c_int, P]
     L.fdtdpic_slot_smem_bytes.restype = c_i64

@@ -102,15 +102,18 @@ class Sweep:
     as a CUDA graph, after which ``run()`` replays it.  dft: "tc" (tensor cores, split-BF16x3;
     ``dft_error()`` reports a tensor-core wait that gave up) or "cuda" (FP32 CUDA cores)."""
 
-    def __init__(self, grids, dt, freqs, precision="f32", threads=256, grid_ctas=0, dft="tc"):
+    def __init__(self, grids, dt, freqs, precision="f32", threads=256, grid_ctas=0, dft="tc",
+                 packed=None):
         self.L = lib()
+        if packed is not None:  # a batch already on the device (fdtdpic.device_setup)
+            grids = packed.grids
         self.grids = grids
         self.n = len(grids)
         steps = {g.n_steps for g in grids}
         if len(steps) != 1:
             raise ValueError("a sweep's grids must share their step count (one DFT length)")
         self.S = steps.pop()
-        self.packed = engine.upload(grids, precision)
+        self.packed = engine.upload(grids, precision) if packed is None else packed
         if self.packed.global_idx:
             raise ValueError("every grid of a sweep must fit the resident kernel")
         self.threads, self.grid_ctas = threads, grid_ctas
@@ -133,6 +136,17 @@ class Sweep:
         self.d_tc = (torch.empty(self.tc_bytes, dtype=torch.uint8, device=dev)
                      if dft == "tc" else None)
         self.graph = None
+
+    @classmethod
+    def from_spec(cls, spec, precision="f32", device_setup=True, **kw):
+        """The seeded batch of ``spec``; with device_setup its CPML tables and coefficients are
+        computed by fdtdpic_setup_batch instead of per grid on the host."""
+        if device_setup:
+            from .device_setup import sweep_batch
+            packed, dt = sweep_batch(spec, precision)
+            return cls(None, dt, spec.freqs(), precision=precision, packed=packed, **kw)
+        grids, dt = make_sweep_grids(spec)
+        return cls(grids, dt, spec.freqs(), precision=precision, **kw)
 
     def _enqueue(self, stream):
         self.launch_fields(stream)
