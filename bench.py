@@ -538,7 +538,7 @@ def main():
     ap.add_argument("--extra", default="sweep,serve,knee,large",
                     help="comma-separated extra sections: sweep, serve, knee, large ('' for none)")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
-    ap.add_argument("--knee-rates", default="4,8,16,24,32",
+    ap.add_argument("--knee-rates", default="1,2,4,8,16",
                     help="offered request rates (per second) of the serving knee section")
     ap.add_argument("--knee-seconds", type=float, default=8.0)
     ap.add_argument("--knee-grace", type=float, default=4.0)

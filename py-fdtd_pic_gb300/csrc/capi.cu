@@ -75,10 +75,9 @@ void pic_graph_store(const void *key, size_t len, cudaGraphExec_t exec)
 {
     if (len > sizeof(g_graphs[0].key)) return;
     PicGraphEntry &e = g_graphs[g_graph_next];
-    if (g_graph_next < g_graph_count && e.exec) {
-        cudaDeviceSynchronize();  // the evicted graph may still be running
-        cudaGraphExecDestroy(e.exec);
-    }
+    // an evicted graph may still be running: cudaGraphExecDestroy frees an executable graph that
+    // is in flight when its launches complete, so no device-wide wait is needed here
+    if (g_graph_next < g_graph_count && e.exec) cudaGraphExecDestroy(e.exec);
     memcpy(e.key, key, len);
     e.key_len = len;
     e.exec = exec;

@@ -11,6 +11,11 @@ it, and a request that arrives mid-run joins at the next round.  Rounds are enqu
 the GPU (at most ``max_inflight`` at a time); the host only waits for a round to read back the
 probes of the requests that finished in it.
 
+A beam request whose predicted work would hold one CTA for longer than ``big_ms`` runs instead
+on the streaming PIC kernels (``fdtdpic_run``: every SM on its push, field and re-binning
+steps, CUDA-graph blocks), on a low-priority side stream beside the rounds, which keep a
+high-priority stream; the two paths give the same results bit for bit.
+
 Results do not depend on the mix: a request's arithmetic is fixed by its own inputs and chunk
 boundaries, and beam deposits are exact integer sums.
 
@@ -34,7 +39,7 @@ from . import physics_setup as ps
 from ._lib import F32, F64, INSTANCE_DTYPE, STATE_ARRAYS, check, lib
 from .engine import _dtype, _require_cuda
 from .grid import Grid, lorentz_kerr_grid, pack
-from .pic import C0, Beam, PicBeam, beam_constants
+from .pic import C0, Beam, PicBeam, PicRun, beam_constants
 
 _PTR = "<u8"
 SLOT_DTYPE = np.dtype([
@@ -104,6 +109,16 @@ class Done:
 
 
 @dataclass
+class _Big:
+    """A beam request running on the streaming kernels (side stream)."""
+    req: Request
+    run: object
+    done_ev: object
+    nbytes: int
+    admitted: float
+
+
+@dataclass
 class _Active:
     req: Request
     slot: int
@@ -120,11 +135,14 @@ class Server:
 
     precision: "f32" (default) or "f64"; hbm_budget: bytes of request buffers held at once;
     max_active: requests resident at once (default 2 x the CTAs one round runs); chunk_ms: the
-    target duration of one work item; keep_state: also return final fields and particles."""
+    target duration of one work item; keep_state: also return final fields and particles;
+    big_ms: beam requests predicted to hold one CTA longer than this run on the streaming
+    kernels (None: never), at most max_big at a time."""
 
     def __init__(self, precision="f32", hbm_budget=150e9, max_active=None, chunk_ms=3.0,
                  threads=512, smem_bytes=64 * 1024, max_inflight=2, keep_state=False,
-                 max_admit_per_poll=64, prefetch=128, device=None, clock=time.perf_counter):
+                 max_admit_per_poll=64, prefetch=128, device=None, clock=time.perf_counter,
+                 big_ms=100.0, max_big=2):
         _require_cuda()
         self.L = lib()
         check_slot_layout(self.L)
@@ -141,9 +159,15 @@ class Server:
         self.chunk_ns = chunk_ms * 1e6
         self.max_inflight = max_inflight
         self.max_admit = max_admit_per_poll
+        self.big_ns = None if big_ms is None else float(big_ms) * 1e6
+        self.max_big = max(1, int(max_big))
+        self.a_cell, self.a_cell_global, self.a_part = 2.5, 6.0, 4.0
         self.keep_state = keep_state
         self.clock = clock
-        self.stream = torch.cuda.Stream(device=self.dev)
+        # rounds on a high-priority stream; each streaming-kernel request on a low-priority
+        # stream of its own (its set-up's copies then wait for nothing else)
+        self.stream = torch.cuda.Stream(device=self.dev, priority=-1)
+        self.big: list[_Big] = []
         n = self.max_active
         self.h_slots = torch.zeros(n * SLOT_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
         self.slots_np = self.h_slots.numpy().view(SLOT_DTYPE)
@@ -158,13 +182,20 @@ class Server:
         self._ready_cv = threading.Condition()
         self._prefetch = max(1, int(prefetch))
         self._unadmitted = 0
+        self._closing = False
+        # requests for the streaming kernels are recognised on submission and prepared by a
+        # second thread, at most max_big ahead, so they never hold up the rounds' requests
+        self._big_inbox: queue.Queue = queue.Queue()
+        self._big_ready: collections.deque = collections.deque()
         self._worker = threading.Thread(target=self._prepare_loop, daemon=True)
         self._worker.start()
+        self._big_worker = threading.Thread(target=self._prepare_big_loop, daemon=True)
+        self._big_worker.start()
         self.bytes_in_use = 0
         self.inflight: collections.deque = collections.deque()
         self.done: list[Done] = []
         # cost model: ns per step per CTA = a_cell * (nz+1) * (1 or global factor) + a_part * np
-        self.a_cell, self.a_cell_global, self.a_part = 2.5, 6.0, 4.0
+        # (constants set above, before the preparation threads start)
         self.scale = 1.0
         self.rounds = 0
         self.cell_steps = 0.0
@@ -208,10 +239,46 @@ class Server:
         self._inbox.put(req)
 
     def close(self):
-        """Stop the preparation thread (pending requests are dropped)."""
+        """Stop the preparation threads (pending requests are dropped) and wait for the work
+        already enqueued on the GPU."""
+        self._closing = True
         self._inbox.put(None)
+        self._big_inbox.put(None)
         with self._ready_cv:
             self._ready_cv.notify_all()
+        for t in (self._worker, self._big_worker):
+            t.join(timeout=30.0)
+        for b in self.big:
+            b.done_ev.synchronize()
+        self.stream.synchronize()
+
+    def _is_big(self, req: Request) -> bool:
+        """A beam request whose predicted work would hold one CTA longer than big_ms (from its
+        sizes alone, so it is known on submission)."""
+        if self.big_ns is None or not req.n_part:
+            return False
+        per_step = self.a_part * req.n_part + self.a_cell_global * (req.nz + 1)
+        return per_step * req.n_steps > self.big_ns
+
+    def _prepare_big_loop(self):
+        while True:
+            req = self._big_inbox.get()
+            if req is None:
+                return
+            with self._ready_cv:
+                while len(self._big_ready) >= self.max_big and not self._closing:
+                    self._ready_cv.wait(0.05)
+            try:
+                if req.grid is None:
+                    req.grid = req.grid_fn()
+                if req.beam is None and req.beam_fn is not None:
+                    req.beam = req.beam_fn()
+                req._host, req._error = None, None
+            except Exception as e:  # reported when the request reaches admission
+                req._host, req._error = None, e
+            with self._ready_cv:
+                self._big_ready.append(req)
+                self._ready_cv.notify_all()
 
     def _prepare_loop(self):
         ts = 8 if self.prec == F64 else 4
@@ -220,8 +287,11 @@ class Server:
             req = self._inbox.get()
             if req is None:
                 return
+            if self._is_big(req):
+                self._big_inbox.put(req)
+                continue
             with self._ready_cv:
-                while len(self._ready) >= self._prefetch:
+                while len(self._ready) >= self._prefetch and not self._closing:
                     self._ready_cv.wait(0.05)
             try:
                 if req.grid is None:
@@ -247,14 +317,31 @@ class Server:
                 self._ready_cv.notify_all()
 
     def _admit(self, now):
+        """Admit prepared requests in arrival order while budget allows: streaming-kernel
+        requests while fewer than max_big run, the others while slots are free."""
         admitted = 0
+        while len(self.big) < self.max_big:
+            with self._ready_cv:
+                if not self._big_ready:
+                    break
+                req = self._big_ready[0]
+                need = self.request_bytes(req)
+                if self.bytes_in_use + need > self.budget and (self.active or self.big):
+                    break
+                self._big_ready.popleft()
+                self._ready_cv.notify_all()
+            self._unadmitted -= 1
+            if req._error is not None:
+                raise req._error
+            self._place_big(req, need, now)
+            admitted += 1
         while self.free and admitted < self.max_admit:
             with self._ready_cv:
                 if not self._ready:
                     break
                 req = self._ready[0]
                 need = self.request_bytes(req)
-                if self.bytes_in_use + need > self.budget and self.active:
+                if self.bytes_in_use + need > self.budget and (self.active or self.big):
                     break
                 self._ready.popleft()
                 self._ready_cv.notify_all()
@@ -264,6 +351,54 @@ class Server:
             self._place(req, need, now)
             admitted += 1
         return admitted
+
+    def _place_big(self, req: Request, need: int, now: float):
+        """Run a beam request on the streaming kernels, all its steps enqueued at once on a
+        low-priority stream of its own (graph blocks of 64 steps)."""
+        g = req.grid
+        req._host = None
+        st = torch.cuda.Stream(device=self.dev, priority=0)
+        with torch.cuda.stream(st):
+            run = PicRun(g, req.beam, req.dz, req.dt, req.mu0,
+                         precision="f64" if self.prec == F64 else "f32", path="streaming",
+                         device=self.dev)
+            run.step(g.n_steps, stream=st)
+            ev = torch.cuda.Event()
+            ev.record(st)
+        need += run.scratch_bytes
+        self.bytes_in_use += need
+        self.big.append(_Big(req=req, run=run, done_ev=ev, nbytes=need, admitted=now))
+
+    def _complete_big(self, block=False):
+        """Retire streaming-kernel requests whose work has run (the oldest first when
+        blocking)."""
+        n = 0
+        for b in list(self.big):
+            if not b.done_ev.query():
+                if not block or n:
+                    continue
+                b.done_ev.synchronize()
+            self.big.remove(b)
+            run, g = b.run, b.req.grid
+            st = run.status()
+            status = np.zeros(4, np.int32)
+            status[:2] = st[:2]
+            fields = parts = None
+            if self.keep_state:
+                f = run.fields()
+                jx, jz = run.currents()
+                fields = dict(Ex=f["Ex"], Hy=f["Hy"], Jx=jx, Jz=jz)
+                cell, frac, ux, uz = run.particles()
+                parts = dict(cell=cell, frac=frac, ux=ux, uz=uz)
+            self.done.append(Done(rid=b.req.rid, arrival=b.req.arrival, admitted=b.admitted,
+                                  finished=self.clock(), probes=run.probes(), status=status,
+                                  fields=fields, particles=parts))
+            self.cell_steps += (g.nz + 1) * g.n_steps
+            self.particle_steps += b.req.n_part * g.n_steps
+            self.bytes_in_use -= b.nbytes
+            b.run = None
+            n += 1
+        return n
 
     def _place(self, req: Request, need: int, now: float):
         g = req.grid
@@ -426,7 +561,7 @@ class Server:
         """One scheduling pass: retire finished rounds, admit, enqueue a round if there is
         room in flight.  Returns the number of requests completed in this pass."""
         now = self.clock() if now is None else now
-        n = self._complete(block=False)
+        n = self._complete(block=False) + self._complete_big(block=False)
         self._admit(now)
         while len(self.inflight) >= self.max_inflight:
             n += self._complete(block=True)
@@ -438,10 +573,13 @@ class Server:
 
     def drain(self):
         """Run until every submitted request has completed."""
-        while self.pending or self.active or self.inflight:
+        while self.pending or self.active or self.inflight or self.big:
             self.poll()
             if not self.active and not self.pending:
-                self._complete(block=True)
+                if self.inflight:
+                    self._complete(block=True)
+                else:
+                    self._complete_big(block=True)
             elif not self.active and not self.inflight:
                 with self._ready_cv:  # waiting for the preparation thread
                     if not self._ready:
@@ -464,7 +602,7 @@ class Server:
                 i += 1
             if now >= duration:
                 break
-            if not self.active and not self.pending and not self.inflight:
+            if not self.active and not self.pending and not self.inflight and not self.big:
                 if i >= len(reqs):
                     break
                 time.sleep(min(1e-3, max(0.0, reqs[i].arrival - now)))
@@ -486,7 +624,7 @@ class Server:
                     throughput_rps=len(self.done) / elapsed if elapsed > 0 else 0.0,
                     p50_s=pct(lat, 50), p99_s=pct(lat, 99), service_p50_s=pct(svc, 50),
                     service_p99_s=pct(svc, 99), queue_depth=self.pending,
-                    active=len(self.active), rounds=self.rounds,
+                    active=len(self.active), streaming=len(self.big), rounds=self.rounds,
                     mcell_steps_per_s=self.cell_steps / elapsed / 1e6 if elapsed > 0 else 0.0,
                     mparticle_steps_per_s=self.particle_steps / elapsed / 1e6
                     if elapsed > 0 else 0.0, gpu_busy_s=self.gpu_ms / 1e3)

@@ -139,3 +139,34 @@ def test_hbm_budget_limits_admission():
         srv.poll()
         peak = max(peak, len(srv.active))
     assert peak == 1 and len(srv.done) == 6
+
+
+def test_streaming_side_path_equals_rounds():
+    """Beam requests sent to the streaming kernels (big_ms=0: every beam request) give the slot
+    rounds' results (big_ms=None) bit for bit, mixed with field-only requests."""
+    _torch()
+    import scipy.constants as sc
+    from fdtdpic.pic import make_beam
+    from fdtdpic.server import Request
+    dt = 0.5 * DZ / 299792458.0
+
+    def reqs():
+        return [Request(grid=_grid(700, 500, 300, 400), beam=make_beam(20000, 40, 660, DZ, seed=5),
+                        dz=DZ, dt=dt, mu0=sc.mu_0, rid=0),
+                Request(grid=_grid(900, 400, 400, 500, nzsrc=100), rid=1),
+                Request(grid=_grid(2500, 300, 1000, 1500), beam=make_beam(3000, 40, 2460, DZ, seed=6),
+                        dz=DZ, dt=dt, mu0=sc.mu_0, rid=2)]
+
+    side = _serve(reqs(), big_ms=0.0, chunk_ms=0.2)
+    rounds = _serve(reqs(), big_ms=None, chunk_ms=0.2)
+    assert sorted(side) == sorted(rounds) == [0, 1, 2]
+    for i in range(3):
+        np.testing.assert_array_equal(side[i].probes, rounds[i].probes)
+        np.testing.assert_array_equal(side[i].fields["Ex"], rounds[i].fields["Ex"])
+        assert side[i].status[0] == rounds[i].status[0] and side[i].status[1] == 0
+    for i in (0, 2):
+        np.testing.assert_array_equal(side[i].fields["Jx"], rounds[i].fields["Jx"])
+        for k in ("cell", "frac", "ux", "uz"):
+            np.testing.assert_array_equal(np.asarray(side[i].particles[k], np.float64),
+                                          np.asarray(rounds[i].particles[k], np.float64),
+                                          err_msg=k)
