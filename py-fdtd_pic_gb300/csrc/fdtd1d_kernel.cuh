@@ -197,7 +197,7 @@ struct GlobalStore {
 // them (the loads are in flight together), then runs
 // e_cell / h_cell on the register copies and stores what the update changed.  The same e_cell /
 // h_cell arithmetic as the global-memory store.
-constexpr int FIELD_U = 4;   // H phase
+constexpr int FIELD_U = 8;   // H phase
 constexpr int FIELD_UE = 2;  // E phase (the Kerr solve holds more registers)
 template <typename T>
 struct RegE {

@@ -536,46 +536,48 @@ __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
     int nfb = 0;
     // FIELD_UE cells per thread per pass, their loads (accumulator words, Hy, Ex, Dx) issued before
     // any of them is updated; then per cell: Hyp <- Hy, accumulators cleared, the E phase with -Jx
+    const bool dxm = I.mode != FDTD_MODE_FREESPACE;
     for (int k0 = blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += FIELD_UE * stride) {
         unsigned long long wx[FIELD_UE][W];
-        RegE<T> r[FIELD_UE];
-        int kind[FIELD_UE];
+        T ex[FIELD_UE], hk[FIELD_UE], hkm[FIELD_UE], dx[FIELD_UE];
 #pragma unroll
         for (int u = 0; u < FIELD_UE; ++u) {
             const int k = k0 + u * stride;
-            kind[u] = (k >= 1 && k < n) ? cell_kind(I, k) : CELL_GENERIC;
+            const bool in = k < n;
 #pragma unroll
-            for (int w = 0; w < W; ++w) wx[u][w] = k < n ? a.acc[(size_t)w * n + k] : 0ull;
-            if (kind[u] == CELL_GENERIC) {
-                e_cell_load<T>(I, s, k, n, r[u]);
-            } else {
-                r[u].hk = __ldg(s.hy + k);
-                r[u].hkm = __ldg(s.hy + k - 1);
-                r[u].ex = s.ex[k];
-                r[u].dx = kind[u] == CELL_KERR ? s.dx[k] : T(0);
-            }
+            for (int w = 0; w < W; ++w) wx[u][w] = in ? a.acc[(size_t)w * n + k] : 0ull;
+            hk[u] = in ? __ldg(s.hy + k) : T(0);
+            hkm[u] = (in && k >= 1) ? __ldg(s.hy + k - 1) : T(0);
+            ex[u] = in ? s.ex[k] : T(0);
+            dx[u] = (in && dxm && k >= I.front && k < I.rear) ? s.dx[k] : T(0);
         }
 #pragma unroll
         for (int u = 0; u < FIELD_UE; ++u) {
             const int k = k0 + u * stride;
             if (k >= n) break;
             const T jxk = Fix<T>::join(wx[u], a.jinv, a.jinv_f);
-            if (kind[u] == CELL_VACUUM) {
+            const int kd = k >= 1 ? cell_kind(I, k) : CELL_GENERIC;
+            if (kd == CELL_VACUUM) {
                 // e_cell: ex + ((hk - hkm) - jx) * ue * den, den = 1
-                s.ex[k] = r[u].ex + ((r[u].hk - r[u].hkm) - jxk) * c.ue;
-            } else if (kind[u] == CELL_KERR) {
+                s.ex[k] = ex[u] + ((hk[u] - hkm[u]) - jxk) * c.ue;
+            } else if (kd == CELL_KERR) {
                 // e_cell's slab branch: Dx + ((hk - hkm) - jx) * dtdz * den, the Kerr root, Ex
-                const T dx = r[u].dx + ((r[u].hk - r[u].hkm) - jxk) * c.dtdz;
-                const T A = kr.root(dx, c.eps0, &nfb);
+                const T d = dx[u] + ((hk[u] - hkm[u]) - jxk) * c.dtdz;
+                const T A = kr.root(d, c.eps0, &nfb);
                 if (a.last) gA[k] = A;
-                s.dx[k] = dx;
-                s.ex[k] = dx / (c.e0r + c.e0chi * A);
+                s.dx[k] = d;
+                s.ex[k] = d / (c.e0r + c.e0chi * A);
             } else if (k >= 1) {
-                e_cell<T>(I, c, kr, r[u], k, src_e, src_h, true, jxk, a.last ? gA : nullptr, &nfb,
+                // PML, source and Lorentz cells: the whole e_cell on a register copy (their
+                // polarisation and psi loaded here)
+                const CellUse cu = cell_use(I, k);
+                RegE<T> r{ex[u], hk[u], hkm[u], dx[u], cu.p ? s.p[k] : T(0),
+                          cu.p ? s.pp[k] : T(0), cu.psie ? s.psie[k] : T(0), s.tab, k, s.W};
+                e_cell<T>(I, c, kr, r, k, src_e, src_h, true, jxk, a.last ? gA : nullptr, &nfb,
                           true);
-                e_cell_store<T>(I, s, k, r[u]);
+                e_cell_store<T>(I, s, k, r);
             }
-            a.hyp[k] = r[u].hk;
+            a.hyp[k] = hk[u];
 #pragma unroll
             for (int w = 0; w < W; ++w) a.acc[(size_t)w * n + k] = 0ull;
             if (a.last) {  // Jz words are only deposited on the call's last step
@@ -609,21 +611,28 @@ __global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int stride = gridDim.x * blockDim.x;
     for (int k0 = 1 + gt; k0 < n - 1; k0 += FIELD_U * stride) {
-        RegH<T> r[FIELD_U];
+        T hy[FIELD_U], e0[FIELD_U], e1[FIELD_U];
 #pragma unroll
-        for (int u = 0; u < FIELD_U; ++u) h_cell_load<T>(I, s, k0 + u * stride, n - 1, r[u]);
+        for (int u = 0; u < FIELD_U; ++u) {
+            const int k = k0 + u * stride;
+            const bool in = k < n - 1;
+            hy[u] = in ? s.hy[k] : T(0);
+            e0[u] = in ? __ldg(s.ex + k) : T(0);
+            e1[u] = in ? __ldg(s.ex + k + 1) : T(0);
+        }
 #pragma unroll
         for (int u = 0; u < FIELD_U; ++u) {
             const int k = k0 + u * stride;
             if (k >= n - 1) break;
-            const int kd = cell_kind(I, k);
-            if (kd != CELL_GENERIC) {
+            if (cell_kind(I, k) != CELL_GENERIC) {
                 // h_cell: hy + (ex[k+1] - ex[k]) * uh * den with den = 1 (interior cells are
                 // outside the slab or in a Kerr slab, so uh is the outside value)
-                s.hy[k] = r[u].hy + (r[u].exk1 - r[u].exk) * c.uh;
+                s.hy[k] = hy[u] + (e1[u] - e0[u]) * c.uh;
             } else {
-                h_cell<T>(I, c, r[u], k, src_h);
-                h_cell_store<T>(I, s, k, r[u]);
+                RegH<T> r{hy[u], e0[u], e1[u], cell_use(I, k).psih ? s.psih[k] : T(0), s.tab,
+                          k, s.W};
+                h_cell<T>(I, c, r, k, src_h);
+                h_cell_store<T>(I, s, k, r);
             }
         }
     }
