@@ -262,7 +262,7 @@ def run_ours(args):
         "clocks": clk.summary(),
     }
     for name, fn in (("sweep", bench_sweep), ("serve", bench_serve), ("knee", bench_serve_knee),
-                     ("large", bench_large)):
+                     ("large", bench_large), ("variants", bench_variants)):
         if name in args.extra:
             try:
                 out[name] = fn(args, flush)
@@ -448,6 +448,41 @@ def bench_large(args, flush):
             "status": [int(x) for x in run.status()]}
 
 
+def bench_variants(args, flush):
+    """Varin's one-pass ADE step (fdtdpic_variant_run, FDTD_VAR_VARIN_STEP) over 16 grids of
+    2^22 cells, FP32: each cell reads Jx, P, Gx3, Qx3, Ex and writes Pbar3, Jx, P, Gx3, Qx3
+    (40 B); 2.7 GB per launch, so the inputs stay well above L2 between launches."""
+    import numpy as np
+    import torch
+    from fdtdpic import variants
+    rows_n, n = 16, 1 << 22
+    rec = variants.make_rows(np.full(rows_n, n), n - 1, 0, n, dt=1.6e-12, dz=1e-3,
+                             eps0=8.854e-12, omega0=2 * np.pi * 1.5e9, gamma=2 * np.pi * 1e8, chi1=0.2, chi3=1e-3,
+                             alpha3=0.699999988079071, nl_gamma=2 * np.pi * 3e8,
+                             nl_omega0=2 * np.pi * 4e9)
+    rows = variants.Rows(rec)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    arrs = [torch.randn(rows_n, n, device="cuda", generator=g) * 1e-3 for _ in range(6)]
+    for _ in range(3):
+        variants.varin_step(*arrs, rows)
+    torch.cuda.synchronize()
+    k = 10
+    e0, e1 = _events()
+    e0.record()
+    for _ in range(k):
+        variants.varin_step(*arrs, rows)
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / k
+    alg = rows_n * n * 40
+    peak, kind = _peaks()
+    gbs = alg / (ms * 1e-3) / 1e9
+    return {"workload": "varin_step_16x4194304_f32", "per_launch_ms": round(ms, 4),
+            "bytes_per_launch": alg, "achieved_gbs": round(gbs, 1),
+            "hbm_frac": round(gbs / peak, 3), "peak_source": kind,
+            "finite": bool(torch.isfinite(arrs[1]).all().item())}
+
+
 def _oracle_setup(n_part):
     import numpy as np
     import scipy.constants as sc
@@ -535,8 +570,9 @@ def main():
     ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--extra", default="sweep,serve,knee,large",
-                    help="comma-separated extra sections: sweep, serve, knee, large ('' for none)")
+    ap.add_argument("--extra", default="sweep,serve,knee,large,variants",
+                    help="comma-separated extra sections: sweep, serve, knee, large, variants "
+                         "('' for none)")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--knee-rates", default="1,2,4,8,16",
                     help="offered request rates (per second) of the serving knee section")

@@ -365,6 +365,72 @@ int fdtdpic_slots_run(int precision, FdtdSlot *d_slots, int n_slots, const FdtdS
                       int n_items, int32_t *d_queue, int64_t smem_bytes, int threads_per_cta,
                       int grid_ctas, fdtdpic_stream_t stream);
 
+/* ---- Per-step variants the reference defines but never calls (its call sites are commented
+ * out or absent): the first-order Mur edge update, the JEC polarisation current and Varin's
+ * explicit nonlinear Lorentz/Kerr/Raman ADE.  Each operation updates rows of device arrays
+ * (row r at element r * stride, the row's first n elements) with the reference function's
+ * arithmetic, in its operation order (FP64: the same values; FP32: float arrays and float
+ * arithmetic on coefficients formed in FP64).
+ *
+ *   FDTD_VAR_MUR_EX    MUR1DEx (BaseFDTD11.py:769-788; call sites Solver_Engine.py:187,318,321)
+ *                      a0 = Ex (in/out), a1 = tempTempVarE.  m = (c0 dt - dz)/(c0 dt + dz);
+ *                      Ex[k] = E2[k+1] + m (Ex[k+1] - E2[k]) for k = 1..4, then
+ *                      Ex[k] = E2[k-1] + m (Ex[k-1] - E2[k]) for k = Nz-1 down to Nz-5, each
+ *                      reading Ex as the reference's loops leave it.  Needs 6 <= nz <= n.
+ *   FDTD_VAR_ADE_JX    ADE_JxUpdate (:543-563; call sites Solver_Engine.py:244,302)
+ *                      a0 = Jx (out), a1 = polarisationCurr, a2 = tempVarPol,
+ *                      a3 = tempTempVarPol; cells front-1 .. rear-1;
+ *                      Jx = c (w0E^2 P1 + (gammaE/dt)(P - P1) + (P - 2 P1 + P2)/dt^2),
+ *                      c = 1/(eps0 wp w0E w0j).  Needs 1 <= front, rear <= n.
+ *   FDTD_VAR_VARIN_PBAR ADE_NonLin_Pol_Ex_Pbar (:567-576)
+ *                      a0 = Pbar3 (out), a1 = Ex, a2 = Qx3; cells front .. rear-1;
+ *                      Pbar3 = eps0 (chi1 E + chi3 (alpha3 E^3 + (1 - alpha3) Q E)).
+ *   FDTD_VAR_VARIN_JP  ADE_Lin_Curr_And_Pol_Varin (:579-593)
+ *                      a0 = Jx (in/out), a1 = polarisationCurr (in/out), a2 = Pbar3;
+ *                      J = (A/D) J + (B/D)(Pbar3 - P), then P = P + dt J, with
+ *                      G = gammaE dt/2, A = 1 - G, D = 1 + G, B = w0E^2 dt.
+ *   FDTD_VAR_VARIN_QG  ADE_Nonlin_Q_and_G (:596-607)
+ *                      a0 = Gx3 (in/out), a1 = Qx3 (in/out), a2 = Ex;
+ *                      G = (e/f) G + (h/f)(E^2 - Q), then Q = Q + dt G, with
+ *                      g = nonLin3gammaE dt/2, e = 1 - g, f = 1 + g, h = nonLin3Omega_0E^2 dt.
+ *   FDTD_VAR_VARIN_STEP the three Varin updates of one cell in one pass (PBAR, JP, QG in that
+ *                      order; the same values as the three calls): a0 = Pbar3, a1 = Jx,
+ *                      a2 = polarisationCurr, a3 = Gx3, a4 = Qx3, a5 = Ex.
+ * The Varin ranges need 0 <= front, rear <= n; front >= rear is an empty range. */
+#define FDTD_VAR_MUR_EX 0
+#define FDTD_VAR_ADE_JX 1
+#define FDTD_VAR_VARIN_PBAR 2
+#define FDTD_VAR_VARIN_JP 3
+#define FDTD_VAR_VARIN_QG 4
+#define FDTD_VAR_VARIN_STEP 5
+
+typedef struct FdtdVariantRow {
+    int32_t n;              /* elements of this row's arrays */
+    int32_t nz;             /* Params.Nz (MUR1DEx's right edge) */
+    int32_t front, rear;    /* Params.materialFrontEdge, materialRearEdge */
+    double c0, dt, dz;      /* Params.c0, delT, dz */
+    double eps0;            /* Params.permit_0 */
+    double plasma_freq;     /* Variables.plasmaFreqE */
+    double omega0, gamma;   /* Variables.omega_0E, gammaE */
+    double omega0_j;        /* Variables.omega_0 (read by ADE_JxUpdate only) */
+    double chi1, chi3;      /* Variables.chi1Stat, chi3Stat */
+    double alpha3;          /* Variables.alpha3 (the float32 value) */
+    double nl_gamma;        /* Variables.nonLin3gammaE */
+    double nl_omega0;       /* Variables.nonLin3Omega_0E */
+} FdtdVariantRow;
+
+/* Like fdtdpic_instance_layout, for FdtdVariantRow. */
+int fdtdpic_variant_layout(int64_t *out, int n);
+/* Host-side check of rows for an operation (FDTDPIC_OK or FDTDPIC_ERR_ARG). */
+int fdtdpic_variant_check(int op, int n_rows, const FdtdVariantRow *h_rows, int64_t stride);
+/* Apply operation `op` to n_rows rows.  h_rows (host) is checked as fdtdpic_variant_check does;
+ * d_rows is its device copy, which the kernel reads.  arrays: the operation's device arrays
+ * a0, a1, ... in the order above (FDTDPIC_F32: float, FDTDPIC_F64: double), each holding
+ * n_rows rows of `stride` elements.  Asynchronous on the stream. */
+int fdtdpic_variant_run(int op, int precision, int n_rows, const FdtdVariantRow *h_rows,
+                        const FdtdVariantRow *d_rows, int64_t stride, void *const *arrays,
+                        fdtdpic_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,6 +15,8 @@ It restates, in numpy, the reference's one-off set-up path and drives the FP64 C
 * ``IntegratorNL1D`` / ``IntegratorLinLor1D`` / ``IntegratorFreeSpace1D``
                                                           Solver_Engine.py:142-371
 * ``envSetup`` / ``matSetup``                             Environment_Setup.py:19-166, Material_Def.py:21-120
+* the uncalled per-step variants ``MUR1DEx``, ``ADE_JxUpdate``, ``ADE_NonLin_Pol_Ex_Pbar``,
+  ``ADE_Lin_Curr_And_Pol_Varin``, ``ADE_Nonlin_Q_and_G``  BaseFDTD11.py:543-607, 769-788
 
 Scalars the reference stores in float32 jitclass fields (``courantNo``, ``alpha3``, ``kappaMax``,
 ``r_scale``, ``r_a_scale``, ``alphaMax``, ``epsRe``, ``muRe``, ``Amplitude``, ``Periods``;
@@ -768,3 +770,56 @@ def integrate_pic(P: RefParams, mode, Exs, Hys, cell, frac, ux, uz, consts, clo,
     return dict(Ex=st["Ex"], Hy=st["Hy"], Dx=st["Dx"], P=st["P"], Acubic=st["A"],
                 psi_Ex=st["psiE"], psi_Hy=st["psiH"], Jx=st["Jx"], Jz=Jz, Hyp=Hyp,
                 probes=pr[:T], lost=lost, plasmaFreqE=float(pf))
+
+
+# ---- the reference's uncalled per-step variants (one grid's arrays, updated in place) ---------
+# Scalar Python arithmetic in the reference's operation order (left to right); the cell loops
+# are vectorised where cells are independent (numpy's elementwise products and sums round one
+# by one, as the reference's scalar ones do).
+
+
+def mur1d_ex(ex, e2, Nz, c0, dt, dz):
+    """MUR1DEx (BaseFDTD11.py:769-788): the two loops in the reference's order."""
+    m = (c0 * dt - dz) / (c0 * dt + dz)
+    for k in range(1, 5):
+        ex[k] = e2[k + 1] + m * (ex[k + 1] - e2[k])
+    for k in range(Nz - 1, Nz - 6, -1):
+        ex[k] = e2[k - 1] + m * (ex[k - 1] - e2[k])
+    return ex
+
+
+def ade_jx_update(jx, pc, p1, p2, front, rear, eps0, wp, w0e, w0j, gamma, dt):
+    """ADE_JxUpdate (BaseFDTD11.py:543-563), cells front-1 .. rear-1."""
+    coef = 1 / (eps0 * wp * w0e * w0j)
+    s = slice(front - 1, rear)
+    jx[s] = coef * (w0e * w0e * p1[s] + (gamma / dt) * (pc[s] - p1[s]) +
+                    (pc[s] - 2 * p1[s] + p2[s]) / (dt * dt))
+    return jx
+
+
+def varin_pbar(pbar, ex, q, front, rear, eps0, chi1, chi3, alpha3):
+    """ADE_NonLin_Pol_Ex_Pbar (BaseFDTD11.py:567-576), cells front .. rear-1."""
+    s = slice(front, rear)
+    E = ex[s]
+    pbar[s] = eps0 * (chi1 * E + chi3 * (alpha3 * E * E * E + (1 - alpha3) * q[s] * E))
+    return pbar
+
+
+def varin_jp(jx, pc, pbar, front, rear, w0e, gamma, dt):
+    """ADE_Lin_Curr_And_Pol_Varin (BaseFDTD11.py:579-593), cells front .. rear-1."""
+    G = (gamma * dt) / 2
+    A, D, B = 1 - G, 1 + G, w0e * w0e * dt
+    s = slice(front, rear)
+    jx[s] = (A / D) * jx[s] + (B / D) * (pbar[s] - pc[s])
+    pc[s] = pc[s] + dt * jx[s]
+    return jx, pc
+
+
+def varin_qg(g, q, ex, front, rear, nl_gamma, nl_w0, dt):
+    """ADE_Nonlin_Q_and_G (BaseFDTD11.py:596-607), cells front .. rear-1."""
+    Gm = (nl_gamma * dt) / 2
+    e, f, h = 1 - Gm, 1 + Gm, nl_w0 * nl_w0 * dt
+    s = slice(front, rear)
+    g[s] = (e / f) * g[s] + (h / f) * (ex[s] * ex[s] - q[s])
+    q[s] = q[s] + dt * g[s]
+    return g, q

@@ -32,6 +32,7 @@ UNITS = {
     "slot.cu": ["-fmad=false"],  # beam requests round as fdtdpic_run's step
     "noalloc.cu": [],
     "setup.cu": ["-fmad=false"],  # set-up products and sums round one by one, as numpy's
+    "variants.cu": ["-fmad=false"],  # the uncalled ADE variants, rounded as the reference's
 }
 
 
@@ -109,6 +110,13 @@ SETUP_FIELDS = ["dz", "dt", "courant", "eps0", "mu0", "char_imp", "eps_re", "mu_
 SETUP_DTYPE = np.dtype([(n, "<f8") for n in SETUP_FIELDS] + [("free_space", "<i4"),
                                                             ("reserved", "<i4")], align=True)
 
+# FdtdVariantRow (include/fdtdpic.h): one row of fdtdpic_variant_run
+VARIANT_FIELDS = ["c0", "dt", "dz", "eps0", "plasma_freq", "omega0", "gamma", "omega0_j", "chi1",
+                  "chi3", "alpha3", "nl_gamma", "nl_omega0"]
+VARIANT_DTYPE = np.dtype([(n, "<i4") for n in ("n", "nz", "front", "rear")] +
+                         [(n, "<f8") for n in VARIANT_FIELDS], align=True)
+VAR_MUR_EX, VAR_ADE_JX, VAR_VARIN_PBAR, VAR_VARIN_JP, VAR_VARIN_QG, VAR_VARIN_STEP = range(6)
+
 MODE_FREESPACE, MODE_LINLOR, MODE_KERR = 0, 1, 2
 F64, F32 = 8, 4
 TAB_ROWS = 8
@@ -173,6 +181,12 @@ def _declare(L):
     L.fdtdpic_setup_layout.argtypes = [P, c_int]
     L.fdtdpic_setup_batch.restype = c_int
     L.fdtdpic_setup_batch.argtypes = [c_int, P, P, P, P]
+    L.fdtdpic_variant_layout.restype = c_int
+    L.fdtdpic_variant_layout.argtypes = [P, c_int]
+    L.fdtdpic_variant_check.restype = c_int
+    L.fdtdpic_variant_check.argtypes = [c_int, c_int, P, c_i64]
+    L.fdtdpic_variant_run.restype = c_int
+    L.fdtdpic_variant_run.argtypes = [c_int, c_int, c_int, P, P, c_i64, P, P]
     L.fdtdpic_slot_check.restype = c_int
     L.fdtdpic_slot_check.argtypes = [c_int, P]
     L.fdtdpic_slot_smem_bytes.restype = c_i64
@@ -223,6 +237,12 @@ def _check_layout(L):
     want = [INSTANCE_DTYPE.itemsize] + [INSTANCE_DTYPE.fields[f][1] for f in INSTANCE_FIELDS]
     if list(out) != want:
         raise RuntimeError(f"FdtdInstance layout mismatch: C {list(out)} vs numpy {want}")
+    n = L.fdtdpic_variant_layout(None, 0)
+    out = np.zeros(n, np.int64)
+    L.fdtdpic_variant_layout(out.ctypes.data, n)
+    want = [VARIANT_DTYPE.itemsize] + [VARIANT_DTYPE.fields[f][1] for f in VARIANT_DTYPE.names]
+    if list(out) != want:
+        raise RuntimeError(f"FdtdVariantRow layout mismatch: C {list(out)} vs numpy {want}")
 
 
 def check(rc, what=""):

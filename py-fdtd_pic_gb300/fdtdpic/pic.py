@@ -178,7 +178,7 @@ class PicRun:
 
 
 def large_case(nz=1 << 24, n_part=64 << 20, total=20000, dz=0.015, nzsrc=100, precision="f32",
-               sort_every=32, path="auto"):
+               sort_every=32, path="auto", chunk=0):
     """The large single-instance workload: ``nz`` cells, ``n_part`` macroparticles spread over
     the whole grid, a Kerr slab over the middle half, ``total`` steps (at the default sizes:
     2^24 cells, 64M particles, 20,000 steps, FP32)."""
@@ -189,7 +189,7 @@ def large_case(nz=1 << 24, n_part=64 << 20, total=20000, dz=0.015, nzsrc=100, pr
                           probes=(50, nz - 50), chi3=1e-2)
     beam = make_beam(n_part, 50, nz - 51, dz, seed=7, sort=False)
     return PicRun(g, beam, dz, 0.5 * dz / C0, sc.mu_0, precision=precision,
-                  sort_every=sort_every, path=path)
+                  sort_every=sort_every, chunk=chunk, path=path)
 
 
 def _main(argv=None):
@@ -205,9 +205,10 @@ def _main(argv=None):
     ap.add_argument("--warmup", type=int, default=64)
     ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
     ap.add_argument("--path", choices=["auto", "streaming", "tiled"], default="auto")
+    ap.add_argument("--chunk", type=int, default=0, help="particles per push CTA (0: default)")
     a = ap.parse_args(argv)
     run = large_case(a.nz, a.particles, a.warmup + 2 * a.steps, precision=a.precision,
-                     path=a.path)
+                     path=a.path, chunk=a.chunk)
     run.step(a.warmup)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()

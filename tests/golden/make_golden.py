@@ -20,7 +20,8 @@ runnable without changing a line of it:
   (``CubicEquationSolver.py:29``), so ``CubicSolver`` packs its four arguments and ``solve``
   unpacks them.  Nothing else in the reference is patched.
 
-Run from the repository root:  ``python tests/golden/make_golden.py`` (about two minutes).
+Run from the repository root:  ``python tests/golden/make_golden.py`` (about two minutes;
+``python tests/golden/make_golden.py variants`` writes ``variants.npz`` alone).
 It reads the reference from ``/root/reference`` (or ``$PYFDTD_REFERENCE``) and writes
 ``*.npz`` beside this file.  The fixtures are committed; tests only read them.
 """
@@ -349,7 +350,86 @@ def stab_cases():
     return dict(stab_in=np.array(ins, float), stab_out=np.array(outs, float))
 
 
-def main():
+VARIANT_CASES = [  # (tag, Nz, materialFrontEdge, materialRearEdge)
+    ("v60", 60, 20, 45), ("v200", 200, 80, 150), ("v6", 6, 1, 5), ("v8", 8, 2, 7),
+    ("v10", 10, 3, 9)]
+
+
+def variant_cases(mods):
+    """The per-step functions no integrator calls (BaseFDTD11.py:543-607, 769-788), each run
+    once on seeded arrays of Nz+1 cells.  Grids of 6-10 cells make MUR1DEx's two loops overlap.
+    ADE_JxUpdate reads V.omega_0, which Variables lacks: the first call's AttributeError is
+    recorded, then the attribute is set and the call repeated."""
+    Variables, Params = mods["classes"][:2]
+    B11 = mods["B11"]
+    rng = np.random.Generator(np.random.PCG64(20261204))
+    out = {}
+    for tag, Nz, front, rear in VARIANT_CASES:
+        P = make_params(Params, Nz=Nz, steps=16, dz=1e-3, sc=0.95, front=front, rear=rear,
+                        pml=1, nzsrc=1, x1=1, x2=1, freq_in=9e9)
+        V = Variables(Nz, 16, 4, 1)
+        n = Nz + 1
+        w0 = 2 * np.pi * rng.uniform(5e9, 20e9)
+        V.omega_0E = w0
+        V.plasmaFreqE = np.sqrt(rng.uniform(1.2, 3.0)) * w0
+        V.gammaE = w0 * rng.uniform(0.01, 0.2)
+        V.chi1Stat = rng.uniform(0.05, 0.5)
+        V.chi3Stat = rng.uniform(1e-4, 1e-2)
+        V.alpha3 = rng.uniform(0.3, 0.9)
+        V.nonLin3gammaE = 0.0 if tag == "v60" else 2 * np.pi * rng.uniform(1e8, 1e9)
+        V.nonLin3Omega_0E = 2 * np.pi * rng.uniform(1e9, 1e10)
+        rec = dict(Nz=Nz, front=front, rear=rear, c0=P.c0, delT=P.delT, dz=P.dz,
+                   permit_0=P.permit_0, omega_0E=V.omega_0E, plasmaFreqE=V.plasmaFreqE,
+                   gammaE=V.gammaE, chi1Stat=V.chi1Stat, chi3Stat=V.chi3Stat, alpha3=V.alpha3,
+                   nonLin3gammaE=V.nonLin3gammaE, nonLin3Omega_0E=V.nonLin3Omega_0E)
+        # MUR1DEx
+        V.Ex = rng.standard_normal(n)
+        V.tempTempVarE = rng.standard_normal(n)
+        rec.update(mur_Ex_in=V.Ex.copy(), mur_E2=V.tempTempVarE.copy())
+        rec["mur_Ex_out"] = np.asarray(B11.MUR1DEx(V, P, None, None), float).copy()
+        # ADE_JxUpdate
+        scale = P.permit_0
+        V.Jx = rng.standard_normal(n)
+        V.polarisationCurr = scale * rng.standard_normal(n)
+        V.tempVarPol = scale * rng.standard_normal(n)
+        V.tempTempVarPol = scale * rng.standard_normal(n)
+        rec.update(jx_in=V.Jx.copy(), jx_pc=V.polarisationCurr.copy(), jx_p1=V.tempVarPol.copy(),
+                   jx_p2=V.tempTempVarPol.copy())
+        try:
+            B11.ADE_JxUpdate(V, P, None, None)
+            rec["jx_raises"] = False
+        except AttributeError:
+            rec["jx_raises"] = True
+        V.omega_0 = 2 * np.pi * rng.uniform(1e9, 1e10)
+        rec["omega_0"] = V.omega_0
+        rec["jx_out"] = np.asarray(B11.ADE_JxUpdate(V, P, None, None), float).copy()
+        # Varin: Pbar3 (entered at zero: the reference stops in the debugger otherwise), then
+        # J and P, then G and Q
+        V.Pbar3 = np.zeros(n)
+        V.Ex = rng.standard_normal(n)
+        V.Qx3 = rng.standard_normal(n) ** 2
+        rec.update(pbar_Ex=V.Ex.copy(), pbar_Q=V.Qx3.copy())
+        rec["pbar_out"] = np.asarray(B11.ADE_NonLin_Pol_Ex_Pbar(V, P), float).copy()
+        V.Jx = rng.standard_normal(n)
+        V.polarisationCurr = scale * rng.standard_normal(n)
+        rec.update(jp_J=V.Jx.copy(), jp_P=V.polarisationCurr.copy())
+        J, Pc = B11.ADE_Lin_Curr_And_Pol_Varin(V, P)
+        rec.update(jp_J_out=np.asarray(J, float).copy(), jp_P_out=np.asarray(Pc, float).copy())
+        V.Gx3 = rng.standard_normal(n)
+        rec.update(qg_G=V.Gx3.copy(), qg_Q=V.Qx3.copy(), qg_Ex=V.Ex.copy())
+        G, Q, _ = B11.ADE_Nonlin_Q_and_G(V, P)
+        rec.update(qg_G_out=np.asarray(G, float).copy(), qg_Q_out=np.asarray(Q, float).copy())
+        for k, v in rec.items():
+            out[f"{tag}_{k}"] = v
+    return out
+
+
+def _no_debugger(*args, **kwargs):
+    raise RuntimeError("the reference reached breakpoint() (a state its checks stop on)")
+
+
+def main(only=None):
+    sys.breakpointhook = _no_debugger
     raw_solve = _install_stubs()
     import BaseFDTD11 as B11
     import Solver_Engine as SE
@@ -358,6 +438,11 @@ def main():
     meta = dict(numpy=np.__version__, scipy=scipy.__version__,
                 eps0=scipy.constants.epsilon_0, mu0=scipy.constants.mu_0)
 
+    if only == "variants" or only is None:
+        np.savez_compressed(os.path.join(OUT, "variants.npz"), **variant_cases(mods), **meta)
+        print("variants done", flush=True)
+        if only == "variants":
+            return
     np.savez_compressed(os.path.join(OUT, "cubic_solve.npz"), **cubic_cases(raw_solve), **meta)
     np.savez_compressed(os.path.join(OUT, "setup.npz"), **env_cases(), **stab_cases(), **meta)
 
@@ -438,4 +523,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)
