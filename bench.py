@@ -457,9 +457,9 @@ def bench_variants(args, flush):
     from fdtdpic import variants
     rows_n, n = 16, 1 << 22
     rec = variants.make_rows(np.full(rows_n, n), n - 1, 0, n, dt=1.6e-12, dz=1e-3,
-                             eps0=8.854e-12, omega0=2 * np.pi * 1.5e9, gamma=2 * np.pi * 1e8, chi1=0.2, chi3=1e-3,
-                             alpha3=0.699999988079071, nl_gamma=2 * np.pi * 3e8,
-                             nl_omega0=2 * np.pi * 4e9)
+                             eps0=8.854e-12, omega0=2 * np.pi * 1.5e9, gamma=2 * np.pi * 1e8,
+                             chi1=0.2, chi3=1e-3, alpha3=0.699999988079071,
+                             nl_gamma=2 * np.pi * 3e8, nl_omega0=2 * np.pi * 4e9)
     rows = variants.Rows(rec)
     g = torch.Generator(device="cuda").manual_seed(3)
     arrs = [torch.randn(rows_n, n, device="cuda", generator=g) * 1e-3 for _ in range(6)]
