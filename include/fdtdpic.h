@@ -205,6 +205,14 @@ int fdtdpic_reflection_ratio(const double *d_X, int n_pairs, int F, double *d_ra
  * Dx) update.  Deposits are exact int64 fixed-point sums (scale jscale), so results do not depend
  * on particle order or thread scheduling; particles are re-binned by cell every sort_every
  * steps so each CTA's deposits stay in a small shared-memory window. */
+/* PicBeam.path: the low bits select the path (FDTDPIC_PATH_MODE); FDTDPIC_PATH_CELLS_INSIDE is
+ * the caller's guarantee that every particle's cell lies in [clo, chi) on entry (the wrap keeps
+ * them there).  With it, when no node clo-1 .. chi is in a PML column, the streaming path may
+ * carry each step's H phase in the next step's push launch (the push then forms H^(t+1/2) at its
+ * nodes itself), taking one dependent launch out of each step; same results. */
+#define FDTDPIC_PATH_MODE 15
+#define FDTDPIC_PATH_CELLS_INSIDE 16
+
 typedef struct PicBeam {
     int32_t n_part;     /* macroparticles */
     int32_t clo, chi;   /* periodic beam domain, cells [clo, chi); 2 <= clo < chi <= nz-2 */
@@ -212,7 +220,8 @@ typedef struct PicBeam {
     int32_t chunk;      /* particles per CTA in the push kernel (0: library default) */
     int32_t path;       /* 0: automatic (= streaming, measured faster on GB300 at every size
                            but the smallest, where the two tie), 1: streaming kernels,
-                           2: persistent tiled kernel */
+                           2: persistent tiled kernel; may be or-ed with
+                           FDTDPIC_PATH_CELLS_INSIDE */
     double kE;     /* q dt / (2 m c) */
     double kH;     /* -q mu0 dt / (2 m) */
     double sc;     /* c dt / dz */

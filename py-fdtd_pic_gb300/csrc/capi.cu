@@ -49,7 +49,7 @@ static TileGeom tiled_geometry(int precision, const FdtdInstance &h, const PicBe
 {
     TileGeom g{};
     int dev = 0, sms = 0, max_optin = 0;
-    if (b.path != 2 || cudaGetDevice(&dev) != cudaSuccess ||
+    if ((b.path & FDTDPIC_PATH_MODE) != 2 || cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
             cudaSuccess)
@@ -285,7 +285,9 @@ int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d
         return FDTDPIC_ERR_ARG;
     if (b.n_part > 0 && (!d_cell || !d_frac || !d_ux || !d_uz || !d_id)) return FDTDPIC_ERR_ARG;
     if (precision != FDTDPIC_F64 && precision != FDTDPIC_F32) return FDTDPIC_ERR_ARG;
-    if (b.path < 0 || b.path > 2) return FDTDPIC_ERR_ARG;
+    if ((b.path & ~(FDTDPIC_PATH_MODE | FDTDPIC_PATH_CELLS_INSIDE)) != 0 ||
+        (b.path & FDTDPIC_PATH_MODE) > 2)
+        return FDTDPIC_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     unsigned char *scr = (unsigned char *)d_scratch;
     const TileGeom tg = tiled_geometry(precision, *h_inst, b);
@@ -304,7 +306,7 @@ int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d
                                  (float *)d_uz, d_id, (float *)d_jx, (float *)d_jz,
                                  (float *)d_hyp, scr, d_status, timing, st);
     }
-    if (b.path == 2) return tg.ok ? FDTDPIC_ERR_OOM : FDTDPIC_ERR_ARG;
+    if ((b.path & FDTDPIC_PATH_MODE) == 2) return tg.ok ? FDTDPIC_ERR_OOM : FDTDPIC_ERR_ARG;
     if (scratch_bytes < fdtdpic_scratch_bytes(precision, h_inst->nz, b.n_part)) return FDTDPIC_ERR_OOM;
     if (precision == FDTDPIC_F64) {
         BatchArgs<double> a{1, d_inst, nullptr, d_pml_tab, d_src, (double *)d_state,

@@ -11,6 +11,7 @@
 // shared-memory window (exact 64-bit adds from pairs of 32-bit shared atomics).
 #pragma once
 #include <cuda_runtime.h>
+#include <limits.h>
 #include <stdint.h>
 
 #include "fdtd1d_kernel.cuh"
@@ -46,6 +47,8 @@ inline cudaError_t launch_pdl(void (*kern)(KArgs...), int grid, int block, cudaS
 
 constexpr int PIC_WIN = 256;      // shared-memory deposit window (nodes) per CTA
 constexpr int PIC_THREADS = 256;  // push kernel CTA size
+constexpr int FIELD_UH_FUSED = 2; // H cells per thread in the push launch's H CTAs (fewer
+                                  // registers than pic_h_kernel's, which the push CTAs share)
 
 // Fixed-point words per current component: FP32 keeps one int64 word (scale 2^S),
 // FP64 two (the remainder below 2^-S kept at a further 2^40).
@@ -121,6 +124,7 @@ struct PicArgs {
     unsigned long long *acc;  // [2*W][nz+1]: Jx words then Jz words
     int32_t *status;
     int deposit_jz;  // Jz (a diagnostic: no field uses it) only on the call's last step
+    int hblocks;     // launches that carry an H phase: its CTAs, ahead of the push CTAs
 };
 
 // One particle's step (everything but the wrap), shared by the streaming and tiled kernels.
@@ -302,132 +306,6 @@ __device__ __forceinline__ void deposit_slot(unsigned long long *win, unsigned l
     }
 }
 
-// The register budget is the compiler's (40 in FP32): capping it at 32 for a full SM of push
-// CTAs left no room for the next kernel's early-launched CTAs (measured slower on one wave of
-// CTAs, no faster on many).
-template <typename T>
-__global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a)
-{
-    constexpr int W = Fix<T>::W;
-    __shared__ unsigned long long win[2 * W * PIC_WIN];
-    __shared__ int base_s;
-    pdl_trigger();
-    const int b0 = blockIdx.x * a.chunk;
-    const int b1 = min(a.n_part, b0 + a.chunk);
-    if (b0 >= b1) return;
-    const int nz1 = a.nz + 1;
-    for (int i = threadIdx.x; i < 2 * W * PIC_WIN; i += blockDim.x) win[i] = 0ull;
-    pdl_wait();  // the previous step's fields and particles
-    // this thread's next particle, loaded one iteration ahead so its loads overlap the current
-    // particle's gathers and push; thread 0's first particle (b0) also places the deposit window
-    int nc = 0;
-    T nf = T(0), nux = T(0), nuz = T(0);
-    if (b0 + (int)threadIdx.x < b1) {
-        const int p = b0 + threadIdx.x;
-        nc = a.cell[p]; nf = a.frac[p]; nux = a.ux[p]; nuz = a.uz[p];
-    }
-    if (threadIdx.x == 0) base_s = nc - 8;
-    __syncthreads();
-    const int base = base_s;
-    const int Lc = a.chi - a.clo;
-    const int iters = (b1 - b0 + blockDim.x - 1) / blockDim.x;
-    const int lane = threadIdx.x & 31;
-    int lost = 0;
-    for (int it = 0; it < iters; ++it) {
-        const int p = b0 + it * blockDim.x + threadIdx.x;
-        bool valid = p < b1;
-        int c = nc;
-        T f = nf;
-        const T ux0 = nux, uz0 = nuz;
-        const int pn = p + blockDim.x;
-        if (pn < b1) { nc = a.cell[pn]; nf = a.frac[pn]; nux = a.ux[pn]; nuz = a.uz[pn]; }
-        if (valid && (c < 1 || c + 2 > a.nz)) { valid = false; ++lost; }
-        int nx0 = -1, nx1 = -1, nzA = -1, nzB = -1;
-        T jx0 = T(0), jx1 = T(0);
-        long long vzA[W], vzB[W];
-#pragma unroll
-        for (int w = 0; w < W; ++w) vzA[w] = vzB[w] = 0;
-        if (valid) {
-            int j;
-            T fh;
-            if (f >= T(0.5)) { j = c; fh = f - T(0.5); } else { j = c - 1; fh = f + T(0.5); }
-            // the fields are read-only during the push: non-coherent loads
-            const T E = (T(1) - f) * __ldg(a.ex + c) + f * __ldg(a.ex + c + 1);
-            const T H = (T(1) - fh) * (T(0.5) * (__ldg(a.hy + j) + __ldg(a.hyp + j))) +
-                        fh * (T(0.5) * (__ldg(a.hy + j + 1) + __ldg(a.hyp + j + 1)));
-            Moved<T> m;
-            particle_step<T>(E, H, c, f, ux0, uz0, a.kE, a.kH, a.sc, a.kJ, m);
-            const T uxn = m.ux, uzn = m.uz, f1 = m.f1;
-            int c1 = m.c1;
-            nx0 = m.nx0;
-            nx1 = m.nx0 + 1;
-            jx0 = m.jx0;
-            jx1 = m.jx1;
-            if (a.deposit_jz) {
-                const MovedJz<T> z = particle_jz<T>(c, f, m, a.kJz);
-                nzA = z.nzA;
-                nzB = z.nzB;
-                Fix<T>::split(z.jzA, a.jscale, a.jscale_f, vzA);
-                if (nzB >= 0) Fix<T>::split(z.jzB, a.jscale, a.jscale_f, vzB);
-            }
-            if (c1 >= a.chi) c1 -= Lc;
-            else if (c1 < a.clo) c1 += Lc;
-            a.cell[p] = c1;
-            a.frac[p] = f1;
-            a.ux[p] = uxn;
-            a.uz[p] = uzn;
-        }
-        // a warp whose Jx values are all zero (particles no field has given transverse momentum)
-        // skips both Jx slots: adding zeros changes nothing
-        if (__any_sync(0xffffffffu, jx0 != T(0) || jx1 != T(0))) {
-            long long vx0[W], vx1[W];
-#pragma unroll
-            for (int w = 0; w < W; ++w) vx0[w] = vx1[w] = 0;
-            if (nx0 >= 0) {
-                Fix<T>::split(jx0, a.jscale, a.jscale_f, vx0);
-                Fix<T>::split(jx1, a.jscale, a.jscale_f, vx1);
-            }
-            // the whole warp on one node pair (a dense beam after re-binning): two warp sums
-            const int i0 = __shfl_sync(0xffffffffu, nx0, 0);
-            const int r0 = i0 - base;
-            if (__all_sync(0xffffffffu, nx0 == i0) && i0 >= 0 && r0 >= 0 && r0 + 1 < PIC_WIN) {
-                // words that fit 32 bits (small currents) take the two-reduction sum
-                bool fit = true;
-#pragma unroll
-                for (int w = 0; w < W; ++w)
-                    fit = fit && vx0[w] == (long long)(int)vx0[w] && vx1[w] == (long long)(int)vx1[w];
-                const bool fit_all = __all_sync(0xffffffffu, fit);
-#pragma unroll
-                for (int w = 0; w < W; ++w) {
-                    const unsigned long long s0 = fit_all ? warp_sum_i32((int)vx0[w])
-                                                          : warp_sum_u64((unsigned long long)vx0[w]);
-                    const unsigned long long s1 = fit_all ? warp_sum_i32((int)vx1[w])
-                                                          : warp_sum_u64((unsigned long long)vx1[w]);
-                    if (lane == 0) {
-                        if (s0 != 0ull) smem_add_u64(win + (size_t)w * PIC_WIN + r0, s0);
-                        if (s1 != 0ull) smem_add_u64(win + (size_t)w * PIC_WIN + r0 + 1, s1);
-                    }
-                }
-            } else {
-                deposit_slot<W>(win, a.acc, nz1, base, 0, nx0, vx0);
-                deposit_slot<W>(win, a.acc, nz1, base, 0, nx1, vx1);
-            }
-        }
-        if (a.deposit_jz) {
-            deposit_slot<W>(win, a.acc, nz1, base, W, nzA, vzA);
-            deposit_slot<W>(win, a.acc, nz1, base, W, nzB, vzB);
-        }
-    }
-    if (lost) atomicAdd(a.status, lost);
-    __syncthreads();
-    for (int i = threadIdx.x; i < 2 * W * PIC_WIN; i += blockDim.x) {
-        const unsigned long long v = win[i];
-        const int word = i / PIC_WIN;
-        const int node = base + (i % PIC_WIN);
-        if (v != 0ull && node >= 0 && node < nz1) atomicAdd(a.acc + (size_t)word * nz1 + node, v);
-    }
-}
-
 // The instance's update constants in the state type and its folded FP32 Kerr constants,
 // computed once per call by pic_consts_kernel (the FP64 pipe is narrow; the field kernels then
 // do no FP64 set-up of their own).
@@ -513,8 +391,8 @@ __device__ __forceinline__ void pic_e_cell(PicField<T> &a, const FdtdInstance &I
 }
 
 template <typename T, class S>
-__device__ __forceinline__ void pic_probes(PicField<T> &a, const FdtdInstance &I, S &s, int t,
-                                           int gt, int gstride, int n)
+__device__ __forceinline__ void pic_probes(const PicField<T> &a, const FdtdInstance &I, S &s,
+                                           int t, int gt, int gstride, int n)
 {
     if (gt < 2 && t >= I.probe_lo[gt] && t <= I.probe_hi[gt])
         a.f.probe[I.probe_offset + (int64_t)t * 2 + gt] = s.Ex(I.probe_cell[gt]);
@@ -607,10 +485,12 @@ __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
     if (nfb && a.f.fallbacks) atomicAdd(a.f.fallbacks, nfb);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
+// The H phase over CTAs hb of nhb (every thread of the CTA calls it): pic_h_kernel's body, and
+// the H part of the push launch that carries the previous step's H phase.  U cells per thread
+// are loaded before any is updated.
+template <typename T, int U>
+__device__ __forceinline__ void pic_h_body(const PicField<T> &a, int t_arg, int hb, int nhb)
 {
-    pdl_trigger();
     const FdtdInstance &I = instance_block(a.f.inst[0]);
     GlobalStore<T, true> s = global_store<T, true>(I, a.f);
     Scal<T> c;
@@ -620,12 +500,12 @@ __global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
     const T src_h = src_h_at<T>(I, a.f.src, t);
     pdl_wait();  // the E phase
     const int n = I.nz + 1;
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const int stride = gridDim.x * blockDim.x;
-    for (int k0 = 1 + gt; k0 < n - 1; k0 += FIELD_U * stride) {
-        T hy[FIELD_U], e0[FIELD_U], e1[FIELD_U];
+    const int gt = hb * blockDim.x + threadIdx.x;
+    const int stride = nhb * blockDim.x;
+    for (int k0 = 1 + gt; k0 < n - 1; k0 += U * stride) {
+        T hy[U], e0[U], e1[U];
 #pragma unroll
-        for (int u = 0; u < FIELD_U; ++u) {
+        for (int u = 0; u < U; ++u) {
             const int k = k0 + u * stride;
             const bool in = k < n - 1;
             hy[u] = in ? s.hy[k] : T(0);
@@ -633,7 +513,7 @@ __global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
             e1[u] = in ? __ldg(s.ex + k + 1) : T(0);
         }
 #pragma unroll
-        for (int u = 0; u < FIELD_U; ++u) {
+        for (int u = 0; u < U; ++u) {
             const int k = k0 + u * stride;
             if (k >= n - 1) break;
             if (cell_kind(I, k) != CELL_GENERIC) {
@@ -650,6 +530,201 @@ __global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
     }
     if (gt == 0) tfsf_edge<T>(I, s, src_h);
     pic_probes<T>(a, I, s, t, gt, stride, n);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
+{
+    pdl_trigger();
+    pic_h_body<T, FIELD_U>(a, t_arg, blockIdx.x, gridDim.x);
+}
+
+// H^(t+1/2) of node k as the H phase computes it (h_cell), from H^(t-1/2) (hyp, which the E
+// phase wrote) and E^t, for nodes outside the PML columns: den = 1 and no psi term, so only the
+// TF/SF correction and the free-space slab's coefficient remain.
+template <typename T>
+struct HOnTheFly {
+    T src_h, uh, uh_slab;
+    int tfsf_cell, slab_lo, slab_hi;
+};
+template <typename T>
+__device__ __forceinline__ T h_on_the_fly(const HOnTheFly<T> &q, int k, T hy, T e0, T e1)
+{
+    if (k == q.tfsf_cell) hy = hy - q.src_h;
+    const T uh = (k >= q.slab_lo && k < q.slab_hi) ? q.uh_slab : q.uh;
+    return hy + (e1 - e0) * uh;
+}
+
+// The register budget is the compiler's (40 in FP32): capping it at 32 for a full SM of push
+// CTAs left no room for the next kernel's early-launched CTAs (measured slower on one wave of
+// CTAs, no faster on many).
+//
+// FUSE_H: the launch also carries the previous step's H phase (hf, step offset th) in its first
+// a.hblocks CTAs, and the push CTAs take H^(t+1/2) at their two nodes from h_on_the_fly
+// instead of reading Hy -- the values the H CTAs write, so the push no longer waits for the H
+// phase and the step's chain is E, then push and H together.  The push CTAs read Hyp and Ex
+// only, which nothing in the launch writes; the host takes this form when every node a particle
+// can gather lies outside the PML columns (fdtdpic_run's beam domain [clo, chi)).
+template <typename T, bool FUSE_H>
+__global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a, PicField<T> hf,
+                                                               int th)
+{
+    constexpr int W = Fix<T>::W;
+    __shared__ unsigned long long win[2 * W * PIC_WIN];
+    __shared__ int base_s;
+    __shared__ HOnTheFly<T> q_s;
+    pdl_trigger();
+    int blk = blockIdx.x;
+    if constexpr (FUSE_H) {
+        if (blk < a.hblocks) {
+            pic_h_body<T, FIELD_UH_FUSED>(hf, th, blk, a.hblocks);
+            return;
+        }
+        blk -= a.hblocks;
+    }
+    const int b0 = blk * a.chunk;
+    const int b1 = min(a.n_part, b0 + a.chunk);
+    if (b0 >= b1) return;
+    const int nz1 = a.nz + 1;
+    for (int i = threadIdx.x; i < 2 * W * PIC_WIN; i += blockDim.x) win[i] = 0ull;
+    if constexpr (FUSE_H) {
+        if (threadIdx.x == 0) {
+            // the constant pool and the instance do not change; the step counter is written by
+            // launches that completed before this one could start
+            const FdtdInstance &I = hf.f.inst[0];
+            HOnTheFly<T> q;
+            q.src_h = src_h_at<T>(I, hf.f.src, pic_step_index(hf, th));
+            q.uh = hf.fc->c.uh;
+            q.uh_slab = hf.fc->c.uh_slab;
+            q.tfsf_cell = I.tfsf ? I.nzsrc - 1 : INT_MIN;
+            const bool fs = I.mode == FDTD_MODE_FREESPACE;
+            q.slab_lo = fs ? I.front : 0;
+            q.slab_hi = fs ? I.rear : 0;
+            q_s = q;
+        }
+    }
+    pdl_wait();  // the previous step's fields and particles
+    // this thread's next particle, loaded one iteration ahead so its loads overlap the current
+    // particle's gathers and push; thread 0's first particle (b0) also places the deposit window
+    int nc = 0;
+    T nf = T(0), nux = T(0), nuz = T(0);
+    if (b0 + (int)threadIdx.x < b1) {
+        const int p = b0 + threadIdx.x;
+        nc = a.cell[p]; nf = a.frac[p]; nux = a.ux[p]; nuz = a.uz[p];
+    }
+    if (threadIdx.x == 0) base_s = nc - 8;
+    __syncthreads();
+    const int base = base_s;
+    const int Lc = a.chi - a.clo;
+    const int iters = (b1 - b0 + blockDim.x - 1) / blockDim.x;
+    const int lane = threadIdx.x & 31;
+    int lost = 0;
+    for (int it = 0; it < iters; ++it) {
+        const int p = b0 + it * blockDim.x + threadIdx.x;
+        bool valid = p < b1;
+        int c = nc;
+        T f = nf;
+        const T ux0 = nux, uz0 = nuz;
+        const int pn = p + blockDim.x;
+        if (pn < b1) { nc = a.cell[pn]; nf = a.frac[pn]; nux = a.ux[pn]; nuz = a.uz[pn]; }
+        if (valid && (c < 1 || c + 2 > a.nz)) { valid = false; ++lost; }
+        int nx0 = -1, nx1 = -1, nzA = -1, nzB = -1;
+        T jx0 = T(0), jx1 = T(0);
+        long long vzA[W], vzB[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) vzA[w] = vzB[w] = 0;
+        if (valid) {
+            int j;
+            T fh;
+            if (f >= T(0.5)) { j = c; fh = f - T(0.5); } else { j = c - 1; fh = f + T(0.5); }
+            // the fields are read-only during the push: non-coherent loads
+            T E, H;
+            if constexpr (FUSE_H) {
+                // E at j..j+2 covers the cells c, c+1 of the E gather and the nodes' updates
+                const T e0 = __ldg(a.ex + j), e1 = __ldg(a.ex + j + 1), e2 = __ldg(a.ex + j + 2);
+                const T p0 = __ldg(a.hyp + j), p1 = __ldg(a.hyp + j + 1);
+                const bool up = j == c;
+                E = (T(1) - f) * (up ? e0 : e1) + f * (up ? e1 : e2);
+                const HOnTheFly<T> &q = q_s;
+                const T n0 = h_on_the_fly<T>(q, j, p0, e0, e1);
+                const T n1 = h_on_the_fly<T>(q, j + 1, p1, e1, e2);
+                H = (T(1) - fh) * (T(0.5) * (n0 + p0)) + fh * (T(0.5) * (n1 + p1));
+            } else {
+                E = (T(1) - f) * __ldg(a.ex + c) + f * __ldg(a.ex + c + 1);
+                H = (T(1) - fh) * (T(0.5) * (__ldg(a.hy + j) + __ldg(a.hyp + j))) +
+                    fh * (T(0.5) * (__ldg(a.hy + j + 1) + __ldg(a.hyp + j + 1)));
+            }
+            Moved<T> m;
+            particle_step<T>(E, H, c, f, ux0, uz0, a.kE, a.kH, a.sc, a.kJ, m);
+            const T uxn = m.ux, uzn = m.uz, f1 = m.f1;
+            int c1 = m.c1;
+            nx0 = m.nx0;
+            nx1 = m.nx0 + 1;
+            jx0 = m.jx0;
+            jx1 = m.jx1;
+            if (a.deposit_jz) {
+                const MovedJz<T> z = particle_jz<T>(c, f, m, a.kJz);
+                nzA = z.nzA;
+                nzB = z.nzB;
+                Fix<T>::split(z.jzA, a.jscale, a.jscale_f, vzA);
+                if (nzB >= 0) Fix<T>::split(z.jzB, a.jscale, a.jscale_f, vzB);
+            }
+            if (c1 >= a.chi) c1 -= Lc;
+            else if (c1 < a.clo) c1 += Lc;
+            a.cell[p] = c1;
+            a.frac[p] = f1;
+            a.ux[p] = uxn;
+            a.uz[p] = uzn;
+        }
+        // a warp whose Jx values are all zero (particles no field has given transverse momentum)
+        // skips both Jx slots: adding zeros changes nothing
+        if (__any_sync(0xffffffffu, jx0 != T(0) || jx1 != T(0))) {
+            long long vx0[W], vx1[W];
+#pragma unroll
+            for (int w = 0; w < W; ++w) vx0[w] = vx1[w] = 0;
+            if (nx0 >= 0) {
+                Fix<T>::split(jx0, a.jscale, a.jscale_f, vx0);
+                Fix<T>::split(jx1, a.jscale, a.jscale_f, vx1);
+            }
+            // the whole warp on one node pair (a dense beam after re-binning): two warp sums
+            const int i0 = __shfl_sync(0xffffffffu, nx0, 0);
+            const int r0 = i0 - base;
+            if (__all_sync(0xffffffffu, nx0 == i0) && i0 >= 0 && r0 >= 0 && r0 + 1 < PIC_WIN) {
+                // words that fit 32 bits (small currents) take the two-reduction sum
+                bool fit = true;
+#pragma unroll
+                for (int w = 0; w < W; ++w)
+                    fit = fit && vx0[w] == (long long)(int)vx0[w] && vx1[w] == (long long)(int)vx1[w];
+                const bool fit_all = __all_sync(0xffffffffu, fit);
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    const unsigned long long s0 = fit_all ? warp_sum_i32((int)vx0[w])
+                                                          : warp_sum_u64((unsigned long long)vx0[w]);
+                    const unsigned long long s1 = fit_all ? warp_sum_i32((int)vx1[w])
+                                                          : warp_sum_u64((unsigned long long)vx1[w]);
+                    if (lane == 0) {
+                        if (s0 != 0ull) smem_add_u64(win + (size_t)w * PIC_WIN + r0, s0);
+                        if (s1 != 0ull) smem_add_u64(win + (size_t)w * PIC_WIN + r0 + 1, s1);
+                    }
+                }
+            } else {
+                deposit_slot<W>(win, a.acc, nz1, base, 0, nx0, vx0);
+                deposit_slot<W>(win, a.acc, nz1, base, 0, nx1, vx1);
+            }
+        }
+        if (a.deposit_jz) {
+            deposit_slot<W>(win, a.acc, nz1, base, W, nzA, vzA);
+            deposit_slot<W>(win, a.acc, nz1, base, W, nzB, vzB);
+        }
+    }
+    if (lost) atomicAdd(a.status, lost);
+    __syncthreads();
+    for (int i = threadIdx.x; i < 2 * W * PIC_WIN; i += blockDim.x) {
+        const unsigned long long v = win[i];
+        const int word = i / PIC_WIN;
+        const int node = base + (i % PIC_WIN);
+        if (v != 0ull && node >= 0 && node < nz1) atomicAdd(a.acc + (size_t)word * nz1 + node, v);
+    }
 }
 
 // The device step counter: set before the first replayed block, advanced by a block's length
@@ -896,6 +971,7 @@ template <typename T>
 struct PicPlan {
     int threads, fblocks, pblocks, sblocks, nz1;
     bool fused;
+    bool fuse_h;  // the push launch carries the previous step's H phase (pic_push_kernel FUSE_H)
     PicArgs<T> pa;
     PicField<T> pf;
     int32_t *counts, *cursor, *step, *tile_sum;
@@ -904,12 +980,35 @@ struct PicPlan {
     T *fracA, *fracB, *uxA, *uxB, *uzA, *uzB;
 };
 
-// Enqueue one step; `sorted` selects which buffer holds the particles (flips when re-binning).
+// A step's H phase not yet launched: the next push launch carries it (fuse_h), or pic_flush_h
+// launches it alone.
+template <typename T>
+struct PendingH {
+    bool on;
+    PicField<T> pf;
+    int t;
+};
+
+template <typename T>
+void pic_flush_h(PicPlan<T> &P, PendingH<T> &ph, cudaStream_t st, PicTimer *tm)
+{
+    if (!ph.on) return;
+    if (tm) tm->begin(&tm->out->field_ms);
+    launch_pdl(pic_h_kernel<T>, P.fblocks, P.threads, st, ph.pf, ph.t);
+    if (tm) tm->end();
+    ph.on = false;
+}
+
+// Enqueue one step; `in_b` selects which buffer holds the particles (flips when re-binning).
+// The step's H phase is left pending in `ph` when the plan fuses it into the next push launch;
+// the caller flushes it after the last step.
 template <typename T>
 void pic_enqueue_step(PicPlan<T> &P, const PicBeam &bm, int t, bool do_sort, bool &in_b,
-                      bool device_step, cudaStream_t st, PicTimer *tm, bool last_step)
+                      bool device_step, cudaStream_t st, PicTimer *tm, bool last_step,
+                      PendingH<T> &ph)
 {
     if (do_sort) {
+        pic_flush_h(P, ph, st, tm);
         int32_t *cS = in_b ? P.cellB : P.cellA, *cD = in_b ? P.cellA : P.cellB;
         int32_t *iS = in_b ? P.idB : P.idA, *iD = in_b ? P.idA : P.idB;
         T *fS = in_b ? P.fracB : P.fracA, *fD = in_b ? P.fracA : P.fracB;
@@ -935,8 +1034,19 @@ void pic_enqueue_step(PicPlan<T> &P, const PicBeam &bm, int t, bool do_sort, boo
     if (bm.n_part > 0) {
         if (tm) tm->begin(&tm->out->push_ms);
         P.pa.deposit_jz = last_step ? 1 : 0;
-        launch_pdl(pic_push_kernel<T>, P.pblocks, PIC_THREADS, st, P.pa);
+        if (ph.on && P.fuse_h) {
+            P.pa.hblocks = P.fblocks;
+            launch_pdl(pic_push_kernel<T, true>, P.fblocks + P.pblocks, PIC_THREADS, st, P.pa,
+                       ph.pf, ph.t);
+            ph.on = false;
+        } else {
+            pic_flush_h(P, ph, st, tm);
+            P.pa.hblocks = 0;
+            launch_pdl(pic_push_kernel<T, false>, P.pblocks, PIC_THREADS, st, P.pa, P.pf, 0);
+        }
         if (tm) tm->end();
+    } else {
+        pic_flush_h(P, ph, st, tm);
     }
     PicField<T> pf = P.pf;
     pf.step = device_step ? P.step : nullptr;
@@ -944,11 +1054,15 @@ void pic_enqueue_step(PicPlan<T> &P, const PicBeam &bm, int t, bool do_sort, boo
     if (tm) tm->begin(&tm->out->field_ms);
     if (P.fused) {
         pic_field_fused_kernel<T><<<1, 1024, 0, st>>>(pf, t);
+        if (tm) tm->end();
     } else {
         launch_pdl(pic_e_kernel<T>, P.fblocks, P.threads, st, pf, t);
-        launch_pdl(pic_h_kernel<T>, P.fblocks, P.threads, st, pf, t);
+        if (tm) tm->end();
+        ph.on = true;
+        ph.pf = pf;
+        ph.t = t;
+        if (!P.fuse_h) pic_flush_h(P, ph, st, tm);
     }
-    if (tm) tm->end();
 }
 
 // Captured step blocks, kept for replay by later calls with identical arguments.
@@ -1006,6 +1120,24 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
     P.pf.jinv = pa.jinv; P.pf.jinv_f = pa.jinv_f; P.pf.step = nullptr; P.pf.last = 0;
     P.pf.fc = (const FieldConsts<T> *)(scratch + L.consts);
     P.pblocks = (bm.n_part + pa.chunk - 1) / pa.chunk;
+    pa.hblocks = 0;
+    {
+        // The push launch carries the previous step's H phase when the caller guarantees the
+        // particles' cells are in [clo, chi), every node a particle can then gather
+        // (clo-1 .. chi) lies strictly inside [1, nz-1] and outside the PML columns
+        // (h_on_the_fly's condition), and the launch is a few waves of push CTAs (its step is
+        // latency-bound; in many-wave launches the push's extra arithmetic costs more than the
+        // launch it saves).  Not when timing kernel by kernel.
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pic_push_kernel<T, true>,
+                                                          PIC_THREADS, 0) != cudaSuccess)
+            per_sm = 0;
+        const long long slots = (long long)per_sm * sms;
+        const bool inside = bm.clo - 1 > h.pml && bm.clo - 1 >= 1 && bm.chi < nz1 - h.pml &&
+                            bm.chi <= h.nz - 1;
+        P.fuse_h = !timing && !P.fused && bm.n_part > 0 && inside && slots > 0 &&
+                   (bm.path & FDTDPIC_PATH_CELLS_INSIDE) && (long long)P.pblocks <= 4 * slots;
+    }
     P.sblocks = (bm.n_part + P.threads - 1) / P.threads;
     if (P.sblocks > 16 * sms) P.sblocks = 16 * sms;
     if (P.sblocks < 1) P.sblocks = 1;
@@ -1053,9 +1185,13 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
             e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
             if (e != cudaSuccess) return cuda_status(e);
             bool cb = false;
+            // a block starts with no H phase pending and ends with its last one launched, so
+            // every replay is the same sequence
+            PendingH<T> bh{};
             for (int j = 0; j < K; ++j)
                 pic_enqueue_step<T>(P, bm, j, sorting && (j % bm.sort_every) == 0, cb, true, cs,
-                                    nullptr, false);
+                                    nullptr, false, bh);
+            pic_flush_h(P, bh, cs, nullptr);
             pic_advance_kernel<<<1, 1, 0, cs>>>(P.step, K);
             cudaGraph_t graph = nullptr;
             e = cudaStreamEndCapture(cs, &graph);
@@ -1072,9 +1208,11 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
         }
         t += nblocks * K;
     }
+    PendingH<T> ph{};
     for (; t < h.step_end; ++t)
         pic_enqueue_step<T>(P, bm, t, sorting && ((t - h.step_begin) % bm.sort_every) == 0, in_b,
-                            false, st, timing ? &tmr : nullptr, t == h.step_end - 1);
+                            false, st, timing ? &tmr : nullptr, t == h.step_end - 1, ph);
+    pic_flush_h(P, ph, st, timing ? &tmr : nullptr);
     if (in_b && bm.n_part > 0) {
         const size_t np = (size_t)bm.n_part;
         e = cudaMemcpyAsync(cell, P.cellB, np * 4, cudaMemcpyDeviceToDevice, st);

@@ -17,6 +17,7 @@ from .engine import _dtype, _ptr, _require_cuda
 from .grid import Grid, pack
 
 C0 = 299792458.0
+PATH_CELLS_INSIDE = 16  # FDTDPIC_PATH_CELLS_INSIDE
 Q_E = -1.602176634e-19
 M_E = 9.1093837139e-31
 
@@ -116,11 +117,20 @@ class PicRun:
         for name, v in self.constants.items():
             setattr(self.pb, name, v)
         self.pb.jscale = self.L.fdtdpic_pic_jscale(ctypes.byref(self.pb))
-        self.pb.path = {"auto": 0, "streaming": 1, "tiled": 2}[path]
+        self.path_mode = {"auto": 0, "streaming": 1, "tiled": 2}[path]
+        self._set_inside(beam)
         self.scratch_bytes = int(self.L.fdtdpic_pic_scratch_bytes(
             self.prec, self.desc.ctypes.data, ctypes.byref(self.pb)))
         self.d_scratch = torch.zeros(max(1, self.scratch_bytes), dtype=torch.uint8, device=dev)
         self.step_done = 0
+
+    def _set_inside(self, beam):
+        # FDTDPIC_PATH_CELLS_INSIDE when every initial cell lies in the beam domain (the wrap
+        # keeps it there), which lets the streaming path overlap each step's H phase with the
+        # next push
+        c = np.asarray(beam.cell)
+        inside = c.size == 0 or (int(c.min()) >= beam.clo and int(c.max()) < beam.chi)
+        self.pb.path = self.path_mode | (PATH_CELLS_INSIDE if inside else 0)
 
     def step(self, n_steps, stream=None, timing=None):
         """Enqueue the next n_steps steps (asynchronous unless ``timing`` is given: then the
@@ -145,6 +155,7 @@ class PicRun:
     def reset(self, beam: Beam | None = None):
         """Back to step 0 with the initial beam (device-to-device; for repeated runs)."""
         b = self.beam if beam is None else beam
+        self._set_inside(b)
         self.d_cell.copy_(torch.from_numpy(np.ascontiguousarray(b.cell, np.int32)))
         self.d_frac.copy_(torch.from_numpy(np.ascontiguousarray(b.frac)))
         self.d_ux.copy_(torch.from_numpy(np.ascontiguousarray(b.ux)))
