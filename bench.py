@@ -229,10 +229,12 @@ def run_ours(args):
             dist.destroy_process_group()
         return None
     # our kernels per run: tiled = init, bin, the persistent kernel, offsets, unbin, status;
-    # streaming = push, E phase and H phase per step, five re-binning kernels (histogram,
-    # three-launch scan, scatter) every 32 steps, the step counter's advance per 64-step graph
-    # block, and init, constants, step-counter set and finish per run
-    launches_per_run = 6 if tiled else 3 * T + 5 * (T // 32) + T // 64 + 4
+    # streaming (this beam lies inside its domain, so each push launch carries the previous
+    # step's H phase) = push and E phase per step, a standalone H phase before each re-binning
+    # and at each block's end (every 32 steps), five re-binning kernels (histogram, three-launch
+    # scan, scatter) every 32 steps, the step counter's advance per 64-step graph block, and
+    # init, constants, step-counter set and finish per run
+    launches_per_run = 6 if tiled else 2 * T + 6 * (T // 32) + T // 64 + 4
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),

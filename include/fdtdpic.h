@@ -234,8 +234,9 @@ typedef struct PicBeam {
  * launch (milliseconds summed over the call).  Passing a timing struct makes the call
  * synchronous and launches kernel by kernel instead of replaying captured graphs. */
 typedef struct FdtdPicTiming {
-    float push_ms;  /* gather + Boris push + deposit */
-    float field_ms; /* field step (E and H phases) */
+    float push_ms;  /* gather + Boris push + deposit (with the previous step's H phase when
+                       the push launch carries it, FDTDPIC_PATH_CELLS_INSIDE) */
+    float field_ms; /* field step (E and H phases; E only where the push carries H) */
     float sort_ms;  /* re-binning by cell */
     int32_t steps;
     int32_t path;   /* 1: streaming kernels, 2: persistent tiled kernel (push_ms = whole kernel) */

@@ -566,8 +566,8 @@ __device__ __forceinline__ T h_on_the_fly(const HOnTheFly<T> &q, int k, T hy, T 
 // only, which nothing in the launch writes; the host takes this form when every node a particle
 // can gather lies outside the PML columns (fdtdpic_run's beam domain [clo, chi)).
 template <typename T, bool FUSE_H>
-__global__ void __launch_bounds__(PIC_THREADS) pic_push_kernel(PicArgs<T> a, PicField<T> hf,
-                                                               int th)
+__global__ void __launch_bounds__(PIC_THREADS, (FUSE_H && sizeof(T) == 4) ? 6 : 1)
+    pic_push_kernel(PicArgs<T> a, PicField<T> hf, int th)
 {
     constexpr int W = Fix<T>::W;
     __shared__ unsigned long long win[2 * W * PIC_WIN];
@@ -1127,7 +1127,7 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
         // (clo-1 .. chi) lies strictly inside [1, nz-1] and outside the PML columns
         // (h_on_the_fly's condition), and the launch is a few waves of push CTAs (its step is
         // latency-bound; in many-wave launches the push's extra arithmetic costs more than the
-        // launch it saves).  Not when timing kernel by kernel.
+        // launch it saves).  Timed kernel by kernel, the fused launch counts as push time.
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pic_push_kernel<T, true>,
                                                           PIC_THREADS, 0) != cudaSuccess)
@@ -1135,8 +1135,14 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
         const long long slots = (long long)per_sm * sms;
         const bool inside = bm.clo - 1 > h.pml && bm.clo - 1 >= 1 && bm.chi < nz1 - h.pml &&
                             bm.chi <= h.nz - 1;
-        P.fuse_h = !timing && !P.fused && bm.n_part > 0 && inside && slots > 0 &&
+        P.fuse_h = !P.fused && bm.n_part > 0 && inside && slots > 0 &&
                    (bm.path & FDTDPIC_PATH_CELLS_INSIDE) && (long long)P.pblocks <= 4 * slots;
+        // a latency-bound step runs faster with fewer particles per thread (768 a CTA measured
+        // best on GB300 for a one-to-two-wave beam; 1024 for many waves)
+        if (P.fuse_h && bm.chunk == 0) {
+            pa.chunk = 768;
+            P.pblocks = (bm.n_part + pa.chunk - 1) / pa.chunk;
+        }
     }
     P.sblocks = (bm.n_part + P.threads - 1) / P.threads;
     if (P.sblocks > 16 * sms) P.sblocks = 16 * sms;
