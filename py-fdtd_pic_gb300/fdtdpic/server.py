@@ -137,12 +137,14 @@ class Server:
     max_active: requests resident at once (default 2 x the CTAs one round runs); chunk_ms: the
     target duration of one work item; keep_state: also return final fields and particles;
     big_ms: beam requests predicted to hold one CTA longer than this run on the streaming
-    kernels (None: never), at most max_big at a time."""
+    kernels (None: never), at most max_big at a time (each such run is latency-bound and holds
+    few SMs, so several share the GPU: on GB300 the served stream's knee moved from 4 to 8 req/s
+    going from 2 to 8 concurrent runs, and 16 gained nothing more)."""
 
     def __init__(self, precision="f32", hbm_budget=150e9, max_active=None, chunk_ms=3.0,
                  threads=512, smem_bytes=64 * 1024, max_inflight=2, keep_state=False,
                  max_admit_per_poll=64, prefetch=128, device=None, clock=time.perf_counter,
-                 big_ms=100.0, max_big=2):
+                 big_ms=100.0, max_big=8):
         _require_cuda()
         self.L = lib()
         check_slot_layout(self.L)
