@@ -586,7 +586,10 @@ __global__ void __launch_bounds__(PIC_THREADS, (FUSE_H && sizeof(T) == 4) ? 6 : 
     const int b1 = min(a.n_part, b0 + a.chunk);
     if (b0 >= b1) return;
     const int nz1 = a.nz + 1;
-    for (int i = threadIdx.x; i < 2 * W * PIC_WIN; i += blockDim.x) win[i] = 0ull;
+    // Jz words are deposited on the call's last step only: other steps clear and flush the
+    // Jx half of the window alone
+    const int win_words = (a.deposit_jz ? 2 : 1) * W * PIC_WIN;
+    for (int i = threadIdx.x; i < win_words; i += blockDim.x) win[i] = 0ull;
     if constexpr (FUSE_H) {
         if (threadIdx.x == 0) {
             // the constant pool and the instance do not change; the step counter is written by
@@ -719,7 +722,7 @@ __global__ void __launch_bounds__(PIC_THREADS, (FUSE_H && sizeof(T) == 4) ? 6 : 
     }
     if (lost) atomicAdd(a.status, lost);
     __syncthreads();
-    for (int i = threadIdx.x; i < 2 * W * PIC_WIN; i += blockDim.x) {
+    for (int i = threadIdx.x; i < win_words; i += blockDim.x) {
         const unsigned long long v = win[i];
         const int word = i / PIC_WIN;
         const int node = base + (i % PIC_WIN);
