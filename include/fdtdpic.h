@@ -239,7 +239,8 @@ typedef struct FdtdPicTiming {
     float field_ms; /* field step (E and H phases; E only where the push carries H) */
     float sort_ms;  /* re-binning by cell */
     int32_t steps;
-    int32_t path;   /* 1: streaming kernels, 2: persistent tiled kernel (push_ms = whole kernel) */
+    int32_t path;   /* 1: streaming kernels, 2: persistent tiled kernel (push_ms = whole kernel),
+                       3: streaming kernels, each push launch carrying the previous H phase */
 } FdtdPicTiming;
 
 /* Bytes of caller scratch fdtdpic_run needs (deposit accumulators, re-binning buffers). */

@@ -1234,7 +1234,7 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
     pic_finish_kernel<T><<<P.fblocks, P.threads, 0, st>>>(fa.state + h.state_offset, nz1, status);
     if (timing) {
         timing->steps = total;
-        timing->path = 1;
+        timing->path = P.fuse_h ? 3 : 1;
         cudaEventDestroy(tmr.ev[0]);
         cudaEventDestroy(tmr.ev[1]);
     }
