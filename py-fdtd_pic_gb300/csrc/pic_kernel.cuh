@@ -546,6 +546,7 @@ template <typename T>
 struct HOnTheFly {
     T src_h, uh, uh_slab;
     int tfsf_cell, slab_lo, slab_hi;
+    int plain;  // no TF/SF cell and no slab coefficient: hy + (e1 - e0) * uh for every node
 };
 template <typename T>
 __device__ __forceinline__ T h_on_the_fly(const HOnTheFly<T> &q, int k, T hy, T e0, T e1)
@@ -603,6 +604,7 @@ __global__ void __launch_bounds__(PIC_THREADS, (FUSE_H && sizeof(T) == 4) ? 6 : 
             const bool fs = I.mode == FDTD_MODE_FREESPACE;
             q.slab_lo = fs ? I.front : 0;
             q.slab_hi = fs ? I.rear : 0;
+            q.plain = !I.tfsf && !fs;
             q_s = q;
         }
     }
@@ -649,8 +651,14 @@ __global__ void __launch_bounds__(PIC_THREADS, (FUSE_H && sizeof(T) == 4) ? 6 : 
                 const bool up = j == c;
                 E = (T(1) - f) * (up ? e0 : e1) + f * (up ? e1 : e2);
                 const HOnTheFly<T> &q = q_s;
-                const T n0 = h_on_the_fly<T>(q, j, p0, e0, e1);
-                const T n1 = h_on_the_fly<T>(q, j + 1, p1, e1, e2);
+                T n0, n1;
+                if (q.plain) {  // the same operations as h_on_the_fly without its two terms
+                    n0 = p0 + (e1 - e0) * q.uh;
+                    n1 = p1 + (e2 - e1) * q.uh;
+                } else {
+                    n0 = h_on_the_fly<T>(q, j, p0, e0, e1);
+                    n1 = h_on_the_fly<T>(q, j + 1, p1, e1, e2);
+                }
                 H = (T(1) - fh) * (T(0.5) * (n0 + p0)) + fh * (T(0.5) * (n1 + p1));
             } else {
                 E = (T(1) - f) * __ldg(a.ex + c) + f * __ldg(a.ex + c + 1);
