@@ -378,8 +378,9 @@ def bench_serve_knee(args, flush):
     """Saturation knee of the server: the served request stream (as in the serve section)
     offered open-loop at each of --knee-rates for --knee-seconds, then polled for --knee-grace
     seconds more without new arrivals.  Per rate: requests completed within that time, their
-    throughput and p50/p99 latency, the backlog left (submitted, not completed) and the GPU busy
-    fraction.  The stream's service times are heavy-tailed (a request of 2M particles and 50k
+    throughput and p50/p99 latency, the backlog left (submitted, not completed) and the fraction
+    of the time the slot rounds kept the GPU busy (the big requests' streaming runs, on streams
+    of their own, are not in it).  The stream's service times are heavy-tailed (a request of 2M particles and 50k
     steps runs for minutes), so the run stops at the grace limit instead of draining.  The knee
     is the highest offered rate at which at least 90% of the requests completed."""
     from fdtdpic import server
@@ -408,7 +409,8 @@ def bench_serve_knee(args, flush):
                      "p50_s": None if st["p50_s"] is None else round(st["p50_s"], 3),
                      "p99_s": None if st["p99_s"] is None else round(st["p99_s"], 3),
                      "backlog": len(reqs) - done,
-                     "gpu_busy": round(st["gpu_busy_s"] / elapsed, 3) if elapsed > 0 else None})
+                     "gpu_busy_rounds": (round(st["gpu_busy_s"] / elapsed, 3)
+                                         if elapsed > 0 else None)})
     knee = max((r["offered_rps"] for r in rows
                 if r["completed_frac"] is not None and r["completed_frac"] >= 0.9), default=None)
     return {"workload": "serve_nz256-65536_steps1k-50k_np0-2M_f32", "window_s": secs,
