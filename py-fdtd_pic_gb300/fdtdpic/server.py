@@ -137,14 +137,16 @@ class Server:
     max_active: requests resident at once (default 2 x the CTAs one round runs); chunk_ms: the
     target duration of one work item; keep_state: also return final fields and particles;
     big_ms: beam requests predicted to hold one CTA longer than this run on the streaming
-    kernels (None: never), at most max_big at a time (each such run is latency-bound and holds
-    few SMs, so several share the GPU: on GB300 the served stream's knee moved from 4 to 8 req/s
-    going from 2 to 8 concurrent runs, and 16 gained nothing more)."""
+    kernels (None: never), at most max_big at a time while no request waits for a slot and at
+    most max_big_busy while some do.  Each streaming run is latency-bound and holds few SMs, so
+    several share an otherwise idle GPU (on GB300 the served stream's knee moved from 4 to 8 req/s
+    going from 2 to 8 concurrent runs, 16 gained nothing), but under overload eight starved the
+    slot rounds (12.8 instead of ~200 req/s completed), hence the lower limit then."""
 
     def __init__(self, precision="f32", hbm_budget=150e9, max_active=None, chunk_ms=3.0,
                  threads=512, smem_bytes=64 * 1024, max_inflight=2, keep_state=False,
                  max_admit_per_poll=64, prefetch=128, device=None, clock=time.perf_counter,
-                 big_ms=100.0, max_big=8):
+                 big_ms=100.0, max_big=8, max_big_busy=2):
         _require_cuda()
         self.L = lib()
         check_slot_layout(self.L)
@@ -163,6 +165,7 @@ class Server:
         self.max_admit = max_admit_per_poll
         self.big_ns = None if big_ms is None else float(big_ms) * 1e6
         self.max_big = max(1, int(max_big))
+        self.max_big_busy = max(1, min(self.max_big, int(max_big_busy)))
         self.a_cell, self.a_cell_global, self.a_part = 2.5, 6.0, 4.0
         self.keep_state = keep_state
         self.clock = clock
@@ -322,7 +325,11 @@ class Server:
         """Admit prepared requests in arrival order while budget allows: streaming-kernel
         requests while fewer than max_big run, the others while slots are free."""
         admitted = 0
-        while len(self.big) < self.max_big:
+        # several streaming runs use an otherwise idle GPU well, but while requests wait for
+        # slots the rounds need the SMs: then at most max_big_busy new runs
+        waiting = bool(self._ready) or not self.free
+        big_limit = self.max_big_busy if waiting else self.max_big
+        while len(self.big) < big_limit:
             with self._ready_cv:
                 if not self._big_ready:
                     break
