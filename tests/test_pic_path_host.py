@@ -1,0 +1,50 @@
+"""Host side of the beam step's path selection (no GPU): PicRun sets FDTDPIC_PATH_CELLS_INSIDE
+exactly when every cell of its host beam lies in [clo, chi), and fdtdpic_run refuses path words
+with unknown bits or an unknown path before any device work (its device pointers here are
+placeholders that a refused call never reads)."""
+import ctypes
+from types import SimpleNamespace
+
+import numpy as np
+
+
+def test_cells_inside_flag_follows_the_host_beam():
+    from fdtdpic.pic import PATH_CELLS_INSIDE, PicBeam, PicRun, make_beam
+    b = make_beam(500, 40, 480, 0.015)
+    for mode in (0, 1, 2):
+        obj = SimpleNamespace(pb=PicBeam(), path_mode=mode)
+        PicRun._set_inside(obj, b)
+        assert obj.pb.path == mode | PATH_CELLS_INSIDE
+    obj = SimpleNamespace(pb=PicBeam(), path_mode=1)
+    for bad in (39, 480, -5, 10_000):
+        c = b.cell.copy()
+        c[7] = bad
+        PicRun._set_inside(obj, SimpleNamespace(cell=c, clo=b.clo, chi=b.chi))
+        assert obj.pb.path == 1, bad
+    PicRun._set_inside(obj, SimpleNamespace(cell=np.zeros(0, np.int32), clo=40, chi=480))
+    assert obj.pb.path == 1 | PATH_CELLS_INSIDE
+
+
+def test_run_refuses_unknown_path_bits():
+    from fdtdpic import _lib
+    from fdtdpic.grid import lorentz_kerr_grid, pack
+    from fdtdpic.pic import PicBeam
+    L = _lib.lib()
+    g = lorentz_kerr_grid(512, 64, front=300, rear=400, nzsrc=60, probes=(50, 350))
+    desc = pack([g], 4)["desc"]
+    fake = ctypes.c_void_p(256)  # never dereferenced: every call below is refused first
+
+    def run(path, scratch_bytes):
+        pb = PicBeam()
+        pb.n_part, pb.clo, pb.chi, pb.sort_every = 0, 40, 480, 32
+        pb.sc, pb.jscale, pb.path = 0.5, 1.0, path
+        return L.fdtdpic_run(_lib.F32, desc.ctypes.data, fake, fake, fake, fake, fake,
+                             ctypes.byref(pb), None, None, None, None, None, fake, fake, fake,
+                             fake, scratch_bytes, fake, None, None)
+
+    for path in (32, 3, 15, 16 | 3, -1):
+        assert run(path, 0) == -1, path  # FDTDPIC_ERR_ARG
+    # accepted path words get past that check to the scratch-size check (FDTDPIC_ERR_OOM),
+    # which also comes before any device work
+    for path in (0, 1, 16, 16 | 1):
+        assert run(path, 0) == -2, path
