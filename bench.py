@@ -250,7 +250,9 @@ def run_ours(args):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(e2e_ms, 3)},
         "roofline": {"bound": "hbm",
-                     "kernel": "pic_tiled_kernel<float>" if tiled else "pic_push_kernel<float>",
+                     "kernel": ("pic_tiled_kernel<float>" if tiled else
+                                "pic_push_kernel<float, FUSE_H> (with the previous step's H phase)"
+                                if tm.path == 3 else "pic_push_kernel<float>"),
                      "path": "tiled" if tiled else "streaming",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 3), "peak_source": peak_kind,
