@@ -21,7 +21,8 @@ runnable without changing a line of it:
   unpacks them.  Nothing else in the reference is patched.
 
 Run from the repository root:  ``python tests/golden/make_golden.py`` (about two minutes;
-``python tests/golden/make_golden.py variants`` writes ``variants.npz`` alone).
+``python tests/golden/make_golden.py variants`` writes ``variants.npz`` alone;
+``python tests/golden/make_golden.py time`` times the reference's own Kerr integrator instead).
 It reads the reference from ``/root/reference`` (or ``$PYFDTD_REFERENCE``) and writes
 ``*.npz`` beside this file.  The fixtures are committed; tests only read them.
 """
@@ -428,12 +429,37 @@ def _no_debugger(*args, **kwargs):
     raise RuntimeError("the reference reached breakpoint() (a state its checks stop on)")
 
 
+def time_reference(mods, n_steps=1024):
+    """Wall time of the reference's own IntegratorNL1D (plain Python here) on the 1000-cell Kerr
+    workload; prints its Mcell-steps/s (the CPU form of the reference's path)."""
+    import time
+    Params = mods["classes"][1]
+    P = make_params(Params, Nz=1000, steps=n_steps, dz=0.015, sc=0.5, front=400, rear=600,
+                    pml=20, nzsrc=100, x1=50, x2=950, freq_in=1e9)
+    P.nonLinMed, P.FreeSpace, P.TFSF = True, False, False
+    src = gauss_sine(P.timeSteps, 1e9, P.delT)
+
+    def cfg0(V):
+        lorentz(V, 2.0, 1.5e9, 2 * np.pi * 0.1e9)
+        V.chi3Stat = 1e-2
+
+    t0 = time.perf_counter()
+    run_case(mods, "IntegratorNL1D", P, cfg0, source=(src, np.zeros_like(src)),
+             keep_history=False)
+    t = time.perf_counter() - t0
+    print(f"reference IntegratorNL1D, Nz=1000, {n_steps} steps: {t:.2f} s, "
+          f"{1001 * n_steps / t / 1e6:.3f} Mcell-steps/s")
+
+
 def main(only=None):
     sys.breakpointhook = _no_debugger
     raw_solve = _install_stubs()
     import BaseFDTD11 as B11
     import Solver_Engine as SE
     mods = dict(classes=_load_state_classes(), SE=SE, B11=B11)
+    if only == "time":
+        time_reference(mods)
+        return
     Variables, Params, CPML_Params, CPML_Variables = mods["classes"]
     meta = dict(numpy=np.__version__, scipy=scipy.__version__,
                 eps0=scipy.constants.epsilon_0, mu0=scipy.constants.mu_0)
