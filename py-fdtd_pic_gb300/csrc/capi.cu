@@ -261,7 +261,8 @@ int64_t fdtdpic_pic_scratch_bytes(int precision, const FdtdInstance *inst, const
     const TileGeom tg = tiled_geometry(precision, *inst, *beam);
     if (tg.ok) {
         const int64_t t = (int64_t)tile_scratch_layout(precision, tg).total;
-        if (beam->path == 2 || t > need) need = (beam->path == 2) ? t : (t > need ? t : need);
+        const bool tiled = (beam->path & FDTDPIC_PATH_MODE) == 2;
+        if (tiled || t > need) need = tiled ? t : (t > need ? t : need);
     }
     return need;
 }
