@@ -325,10 +325,8 @@ class Server:
         """Admit prepared requests in arrival order while budget allows: streaming-kernel
         requests while fewer than max_big run, the others while slots are free."""
         admitted = 0
-        # several streaming runs use an otherwise idle GPU well, but while requests wait for
-        # slots the rounds need the SMs: then at most max_big_busy new runs
-        waiting = bool(self._ready) or not self.free
-        big_limit = self.max_big_busy if waiting else self.max_big
+        big_limit = streaming_limit(bool(self._ready), bool(self.free), self.max_big,
+                                    self.max_big_busy)
         while len(self.big) < big_limit:
             with self._ready_cv:
                 if not self._big_ready:
@@ -642,6 +640,14 @@ class Server:
 # ------------------------------------------------------------------------------------------
 # the served request stream: Poisson arrivals, ragged grids, optional beams
 # ------------------------------------------------------------------------------------------
+def streaming_limit(requests_waiting: bool, slots_free: bool, max_big: int,
+                    max_big_busy: int) -> int:
+    """How many streaming runs big requests may hold: several use an otherwise idle GPU well,
+    but while prepared requests wait for a slot, or no slot is free, the slot rounds need the
+    SMs, so then at most max_big_busy."""
+    return max_big_busy if (requests_waiting or not slots_free) else max_big
+
+
 def make_request_stream(rate=2000.0, duration=60.0, seed=20261203, nz_lo=256, nz_hi=65536,
                         steps_lo=1000, steps_hi=50000, np_max=2_000_000, dz=0.015, sc=0.5,
                         max_requests=None):

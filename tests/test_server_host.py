@@ -65,3 +65,14 @@ def test_request_stream_shapes():
     g = reqs[0].grid_fn()  # grids are built on admission
     assert g.nz == reqs[0].nz and g.n_steps == reqs[0].n_steps
     assert g.front >= 102 and g.rear <= g.nz - 22
+
+
+def test_streaming_limit_drops_while_requests_wait():
+    from fdtdpic.server import streaming_limit
+    # an idle server lets big requests use the GPU with many streaming runs ...
+    assert streaming_limit(False, True, 8, 2) == 8
+    # ... but while prepared requests wait for a slot, or every slot is taken, the slot rounds
+    # need the SMs
+    assert streaming_limit(True, True, 8, 2) == 2
+    assert streaming_limit(False, False, 8, 2) == 2
+    assert streaming_limit(True, False, 8, 2) == 2
