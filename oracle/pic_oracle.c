@@ -47,19 +47,43 @@ int or_pic_step(int n_part, int *cell, double *frac, double *ux, double *uz, con
     const int Lc = chi - clo;
     const int len = nz + 1;
     if (n_threads < 1) n_threads = 1;
-    double *bufs = (double *)calloc((size_t)n_threads * 2 * len, sizeof(double));
-    if (!bufs) return -1;
+    if (n_threads > n_part) n_threads = n_part > 0 ? n_part : 1;
+    /* Thread t takes particles [n_part t / T, n_part (t+1) / T) and deposits into a private
+     * window of cells [lo_t, hi_t] covering every node its particles can reach (c-1 .. c+2):
+     * sorted beams need windows a fraction of the grid long, so large grids stay cheap.  The
+     * windows are summed in thread order below. */
+    int *win = (int *)malloc((size_t)n_threads * 2 * sizeof(int));
+    size_t *off = (size_t *)malloc((size_t)(n_threads + 1) * sizeof(size_t));
+    if (!win || !off) { free(win); free(off); return -1; }
+    off[0] = 0;
+    for (int t = 0; t < n_threads; ++t) {
+        const int p0 = (int)((long long)n_part * t / n_threads);
+        const int p1 = (int)((long long)n_part * (t + 1) / n_threads);
+        int cmin = len, cmax = -1;
+        for (int p = p0; p < p1; ++p) {
+            if (cell[p] < cmin) cmin = cell[p];
+            if (cell[p] > cmax) cmax = cell[p];
+        }
+        int lo = cmin - 1, hi = cmax + 2;
+        if (lo < 0) lo = 0;
+        if (hi > len - 1) hi = len - 1;
+        if (hi < lo) { lo = 0; hi = -1; }
+        win[2 * t] = lo;
+        win[2 * t + 1] = hi;
+        off[t + 1] = off[t] + 2 * (size_t)(hi - lo + 1);
+    }
+    double *bufs = (double *)calloc(off[n_threads] > 0 ? off[n_threads] : 1, sizeof(double));
+    if (!bufs) { free(win); free(off); return -1; }
     int lost = 0;
-#pragma omp parallel num_threads(n_threads) reduction(+ : lost)
-    {
-        int tid = 0;
-#ifdef _OPENMP
-        tid = omp_get_thread_num();
-#endif
-        double *jx = bufs + (size_t)tid * 2 * len;
-        double *jz = jx + len;
-#pragma omp for schedule(static)
-        for (int p = 0; p < n_part; ++p) {
+    /* one partition per loop index, so the result does not depend on the team size */
+#pragma omp parallel for num_threads(n_threads) schedule(static, 1) reduction(+ : lost)
+    for (int t = 0; t < n_threads; ++t) {
+        const int wlo = win[2 * t], wn = win[2 * t + 1] - wlo + 1;
+        double *jx = bufs + off[t] - wlo; /* jx[k], jz[k] for k in [wlo, whi] */
+        double *jz = jx + wn;
+        const int p_begin = (int)((long long)n_part * t / n_threads);
+        const int p_end = (int)((long long)n_part * (t + 1) / n_threads);
+        for (int p = p_begin; p < p_end; ++p) {
             const int c = cell[p];
             const double f = frac[p];
             int j;
@@ -107,15 +131,21 @@ int or_pic_step(int n_part, int *cell, double *frac, double *ux, double *uz, con
             uz[p] = uzn;
         }
     }
+#pragma omp parallel for num_threads(n_threads) schedule(static)
     for (int k = 0; k < len; ++k) {
         double sx = 0.0, sz = 0.0;
         for (int t = 0; t < n_threads; ++t) {
-            sx += bufs[(size_t)t * 2 * len + k];
-            sz += bufs[(size_t)t * 2 * len + len + k];
+            const int wlo = win[2 * t];
+            if (k < wlo || k > win[2 * t + 1]) continue;
+            const int wn = win[2 * t + 1] - wlo + 1;
+            sx += bufs[off[t] + (k - wlo)];
+            sz += bufs[off[t] + wn + (k - wlo)];
         }
         Jx[k] = sx;
         Jz[k] = sz;
     }
     free(bufs);
+    free(win);
+    free(off);
     return lost;
 }

@@ -104,16 +104,17 @@ def test_batch_equals_alone_and_is_deterministic():
 
 
 def test_fp32_error_vs_fp64_oracle():
-    """FP32 state (FP64 only for near-degenerate cubics) against the FP64 oracle."""
+    """FP32 state (FP64 only for near-degenerate cubics) against the reference's FP64 outputs
+    over 4096 steps: 1e-5 relative L2 on the final fields, 5e-5 on the probe traces."""
     for name in ("kerr_nz1000", "lorentz_nz1000"):
         g, grids, res = _run_golden(name, "f32")
         last = res[-1]
-        # FP32 over 4096 steps: stated bound 1e-4 relative L2 on the fields and probes
-        assert O.rel_l2(last.Ex, g["Ex"]) <= 1e-4, name
-        assert O.rel_l2(last.Hy, g["Hy"]) <= 1e-4, name
-        tr = last.probes[:, 1] if name.startswith("kerr") else last.probes[:, 1]
         want = g["Port2"] if name.startswith("kerr") else g["x1ColAf"]
-        assert O.rel_l2(tr, want) <= 1e-4, name
+        e = dict(Ex=O.rel_l2(last.Ex, g["Ex"]), Hy=O.rel_l2(last.Hy, g["Hy"]),
+                 trace=O.rel_l2(last.probes[:, 1], want))
+        print(f"\n{name} FP32 vs reference: " + ", ".join(f"{k} {v:.3e}" for k, v in e.items()))
+        assert e["Ex"] <= 1e-5 and e["Hy"] <= 1e-5, (name, e)
+        assert e["trace"] <= 5e-5, (name, e)
 
 
 def test_cubic_root0_on_gpu_matches_reference_answers():

@@ -1,0 +1,246 @@
+"""Parity at the benchmarked workloads' own sizes, against the FP64 CPU oracle.
+
+* 4096-cell grid + 1,048,576-particle beam (the headline workload): FP64 over its first 512
+  steps on the automatic path (the push launches carry the previous step's H phase), and FP32
+  over all 8192 steps.
+* The 4096-grid ragged sweep (Nz 500-8000, 8192 steps, Kerr): 32 of its grids spanning the Nz
+  range, FP32, fields, probe traces and |R(f)|.
+* The large instance (2^24 cells, 64M particles, Kerr slab over the middle half): 40 steps in
+  FP64 and FP32.
+
+Every measured error is printed (run pytest with -s to see them) beside the bound it is held to.
+FP32 bounds: fields 1e-5 relative L2; probe traces 5e-5 (a trace also holds the low-amplitude
+tail after the pulse has passed, where FP32 rounding is a larger share); |R(f)| 1e-4 of its
+largest value in the source band.  FP64 bounds: 1e-12 on fields and probes, cells equal.
+"""
+import os
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+NZ, T, NP, DZ = 4096, 8192, 1 << 20, 0.015
+DT = 0.5 * DZ / O.C0
+FRONT, REAR, NZSRC, PROBES = 400, 600, 100, (50, 4046)
+CLO, CHI = 50, 4045
+THREADS = max(1, os.cpu_count() or 1)
+
+F64_FIELDS = 1e-12
+F32_FIELDS = 1e-5
+F32_TRACES = 5e-5
+F32_REFL = 1e-4
+
+
+def _torch():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _report(name, errs, bounds):
+    print("\n" + name + ": " + ", ".join(
+        f"{k} {v:.3e} (bound {bounds[k]:.0e})" if k in bounds else f"{k} {v:.3e}"
+        for k, v in errs.items()))
+    for k, b in bounds.items():
+        assert errs[k] <= b, (name, k, errs[k], b)
+
+
+def _ref_params(nz, steps, front, rear, nzsrc, eps0, mu0):
+    return O.RefParams(Nz=nz, timeSteps=steps, dz=DZ, delT=DT, courantNo=O.f32(0.5),
+                       materialFrontEdge=front, materialRearEdge=rear, pmlWidth=20, nzsrc=nzsrc,
+                       freq_in=1e9, permit_0=eps0, permea_0=mu0, nonLinMed=True, FreeSpace=False,
+                       plasmaFreqE=np.sqrt(2.0) * 2 * np.pi * 1.5e9, omega_0E=2 * np.pi * 1.5e9,
+                       gammaE=2 * np.pi * 0.1e9, chi3Stat=1e-2,
+                       sigmaOpt=O.sigma_opt(DZ, eps0, mu0))
+
+
+def _oracle_pic(g, beam, n_steps, probe_cells, front, rear, nzsrc):
+    """The FP64 oracle on the beam (sorted by position for compact per-thread deposit windows;
+    the physics does not depend on particle order).  Particle arrays come back in id order."""
+    import scipy.constants as sc
+    P = _ref_params(g.nz, g.n_steps, front, rear, nzsrc, g.eps0, sc.mu_0)
+    zeta = beam.cell + beam.frac
+    order = np.argsort(zeta, kind="stable")
+    cell = np.ascontiguousarray(beam.cell[order])
+    frac = np.ascontiguousarray(beam.frac[order])
+    ux = np.ascontiguousarray(beam.ux[order])
+    uz = np.ascontiguousarray(beam.uz[order])
+    k = O.pic_constants(DZ, DT, beam.weight, sc.mu_0)
+    r = O.integrate_pic(P, O.KERR, g.exs, np.zeros(g.n_steps), cell, frac, ux, uz, k, beam.clo,
+                        beam.chi, n_steps=n_steps, probe_cells=probe_cells, n_threads=THREADS)
+    ids = beam.id[order]
+    parts = []
+    for a in (cell, frac, ux, uz):
+        out = np.empty_like(a)
+        out[ids] = a
+        parts.append(out)
+    return r, parts
+
+
+def _pic_errors(run, r, parts, n_steps):
+    f = run.fields()
+    jx, jz = run.currents()
+    cell, frac, ux, uz = run.particles()
+    oc, of, oux, ouz = parts
+    pr = run.probes()[:n_steps]
+    return dict(
+        Ex=O.rel_l2(f["Ex"], r["Ex"]), Hy=O.rel_l2(f["Hy"], r["Hy"]),
+        Dx=O.rel_l2(f["Dx"], r["Dx"]),
+        probe0=O.rel_l2(pr[:, 0], r["probes"][:, 0]),
+        probe1=O.rel_l2(pr[:, 1], r["probes"][:, 1]),
+        Jx=O.rel_l2(jx, r["Jx"]), Jz=O.rel_l2(jz, r["Jz"]),
+        zeta=float(np.abs((cell - oc) + (frac - of)).max()),
+        cells_differ=float(np.count_nonzero(cell != oc)),
+        ux=O.rel_l2(ux, oux), uz=O.rel_l2(uz, ouz))
+
+
+def _headline(precision):
+    import scipy.constants as sc
+    from fdtdpic.grid import lorentz_kerr_grid
+    from fdtdpic.pic import PicRun, make_beam
+    g = lorentz_kerr_grid(NZ, T, front=FRONT, rear=REAR, nzsrc=NZSRC, probes=PROBES, chi3=1e-2)
+    beam = make_beam(NP, CLO, CHI, DZ)
+    run = PicRun(g, beam, DZ, DT, sc.mu_0, precision=precision, sort_every=32)
+    return g, beam, run
+
+
+def test_headline_shape_fp64_first_512_steps():
+    """Nz=4096, 2^20 particles, FP64, the automatic path (each push launch carries the previous
+    step's H phase): 480 steps from captured graph blocks, the last 32 launch by launch."""
+    torch = _torch()
+    from fdtdpic.pic import FdtdPicTiming
+    n = 512
+    g, beam, run = _headline("f64")
+    run.step(n - 32)
+    tm = FdtdPicTiming()
+    run.step(32, timing=tm)
+    torch.cuda.synchronize()
+    assert tm.path == 3, "the headline shape should take the fused push-with-H launches"
+    assert int(run.status()[0]) == 0 and int(run.status()[1]) == 0
+    r, parts = _oracle_pic(g, beam, n, PROBES, FRONT, REAR, NZSRC)
+    assert r["lost"] == 0
+    e = _pic_errors(run, r, parts, n)
+    _report("headline FP64, 512 steps", e,
+            dict(Ex=F64_FIELDS, Hy=F64_FIELDS, Dx=F64_FIELDS, probe0=F64_FIELDS,
+                 probe1=F64_FIELDS, Jx=1e-11, Jz=F64_FIELDS, cells_differ=0, zeta=1e-12,
+                 ux=1e-11, uz=1e-14))
+
+
+def test_headline_fp32_all_8192_steps():
+    """The benchmarked run itself (FP32, 8192 steps, graph-replayed streaming path) against the
+    FP64 oracle."""
+    torch = _torch()
+    g, beam, run = _headline("f32")
+    run.step(T)
+    torch.cuda.synchronize()
+    assert int(run.status()[0]) == 0 and int(run.status()[1]) == 0
+    r, parts = _oracle_pic(g, beam, T, PROBES, FRONT, REAR, NZSRC)
+    e = _pic_errors(run, r, parts, T)
+    # particles: a position error of 1e-3 cell and 1e-4 relative on the momenta after 8192
+    # steps (FP32 positions are rounded to 2^-24 of a cell every step)
+    _report("headline FP32, 8192 steps", e,
+            dict(Ex=F32_FIELDS, Hy=F32_FIELDS, Dx=F32_FIELDS, probe0=F32_TRACES,
+                 probe1=F32_TRACES, zeta=1e-3, ux=1e-4, uz=1e-6))
+
+
+def _sweep_sample(n_pick=32):
+    from fdtdpic import sweep
+    spec = sweep.SweepSpec()
+    params = sweep.sweep_parameters(spec)
+    nz = np.array([p["nz"] for p in params])
+    order = np.argsort(nz, kind="stable")
+    pick = sorted(set(int(order[i]) for i in np.linspace(0, len(order) - 1, n_pick).round()))
+    return spec, params, pick
+
+
+def test_sweep_sample_fp32_all_8192_steps():
+    """32 grids of the 4096-grid sweep (its smallest, its largest and 30 between by Nz), FP32,
+    8192 steps, tensor-core DFT, against the FP64 oracle's fields, traces and |R(f)|."""
+    torch = _torch()
+    import scipy.constants as sc
+    from fdtdpic import engine, sweep
+    spec, params, pick = _sweep_sample()
+    grids_all, dt = sweep.make_sweep_grids(spec)
+    grids = [grids_all[i] for i in pick]
+    sw = sweep.Sweep(grids, dt, spec.freqs(), precision="f32", dft="tc")
+    sw.run()
+    torch.cuda.synchronize()
+    assert sw.dft_error() == 0
+    res = engine.download(sw.packed)
+    R = sw.reflection()
+    freqs = spec.freqs()
+    n = np.arange(spec.n_steps)
+    W = np.exp(-2j * np.pi * np.outer(freqs * dt, n))
+
+    def oracle_one(i):
+        p = params[i]
+        w0 = 2 * np.pi * p["f0"]
+        P = O.RefParams(Nz=p["nz"], timeSteps=spec.n_steps, dz=sweep.DZ, delT=dt,
+                        courantNo=O.f32(sweep.SC), materialFrontEdge=p["front"],
+                        materialRearEdge=p["rear"], pmlWidth=spec.pml, nzsrc=spec.nzsrc,
+                        freq_in=spec.freq_in, permit_0=sc.epsilon_0, permea_0=sc.mu_0,
+                        nonLinMed=True, FreeSpace=False, plasmaFreqE=np.sqrt(p["d_eps"]) * w0,
+                        omega_0E=w0, gammaE=2 * np.pi * 0.1e9, chi3Stat=p["chi3"],
+                        sigmaOpt=O.sigma_opt(sweep.DZ, sc.epsilon_0, sc.mu_0))
+        return O.integrate(P, O.KERR, grids_all[i].exs, np.zeros(spec.n_steps),
+                           extra_probes=p["probes"])
+
+    with ThreadPoolExecutor(THREADS) as ex:  # the oracle's C loop releases the GIL
+        refs = list(ex.map(oracle_one, pick))
+    worst = dict(fields=0.0, traces=0.0, refl=0.0)
+    for j, (i, r) in enumerate(zip(pick, refs)):
+        assert res[j].status == 0
+        worst["fields"] = max(worst["fields"], O.rel_l2(res[j].Ex, r.Ex), O.rel_l2(res[j].Hy, r.Hy))
+        for k in (0, 1):
+            worst["traces"] = max(worst["traces"], O.rel_l2(res[j].probes[:, k], r.probes[:, k]))
+        want = r.probes.T @ W.T
+        band = np.abs(want[0]) >= 1e-2 * np.abs(want[0]).max()
+        want_r = np.abs(want[1]) / np.abs(want[0])
+        worst["refl"] = max(worst["refl"], float(np.abs(R[j][band] - want_r[band]).max()
+                                                 / max(want_r[band].max(), 1e-30)))
+    nzs = [params[i]["nz"] for i in pick]
+    print(f"\nsweep sample: {len(pick)} grids, Nz {min(nzs)}..{max(nzs)}")
+    _report("sweep FP32, 8192 steps", worst,
+            dict(fields=F32_FIELDS, traces=F32_TRACES, refl=F32_REFL))
+
+
+@pytest.fixture(scope="module")
+def large_oracle():
+    _torch()
+    from fdtdpic.pic import large_case
+    run = large_case(precision="f64")  # only its grid and beam: the oracle's inputs
+    g, beam = run.grid, run.beam
+    del run
+    import torch
+    torch.cuda.empty_cache()
+    nz = g.nz
+    r, parts = _oracle_pic(g, beam, 40, (50, nz - 50), nz // 4, 3 * nz // 4, 100)
+    return r, parts
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_large_instance_first_40_steps(large_oracle, precision):
+    """2^24 cells, 64M particles (unsorted on entry: the first re-binning orders them), 40
+    steps, against the oracle."""
+    torch = _torch()
+    from fdtdpic.pic import large_case
+    r, parts = large_oracle
+    run = large_case(precision=precision)
+    run.step(40)
+    torch.cuda.synchronize()
+    assert int(run.status()[0]) == 0 and int(run.status()[1]) == 0
+    e = _pic_errors(run, r, parts, 40)
+    del run
+    torch.cuda.empty_cache()
+    if precision == "f64":
+        bounds = dict(Ex=F64_FIELDS, Hy=F64_FIELDS, Dx=F64_FIELDS, probe0=F64_FIELDS,
+                      Jz=F64_FIELDS, cells_differ=0, zeta=1e-12, uz=1e-14)
+    else:
+        bounds = dict(Ex=F32_FIELDS, Hy=F32_FIELDS, Dx=F32_FIELDS, probe0=F32_TRACES,
+                      zeta=1e-4, uz=1e-6)
+    _report(f"large instance {precision.upper()}, 40 steps", e, bounds)
