@@ -276,8 +276,11 @@ int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d
  * every device that loads the library until exit.  Runs needing more scratch than that
  * (fdtdpic_scratch_bytes > 24 MiB) return FDTDPIC_ERR_OOM.  All calls share the array, so calls
  * that overlap on the GPU race: serialise them.  The first call on a device looks up the array's
- * address (make it before any stream capture).  Launches kernel by kernel; no cudaMalloc, no
- * graph capture, no event or stream creation. */
+ * address (make it before any stream capture) and keeps it for the device's context: do not call
+ * this entry point on a device after cudaDeviceReset.  Streaming kernels only: beam->path takes
+ * the bits fdtdpic_run takes with mode 0 or 1 (mode 2, the tiled path, returns
+ * FDTDPIC_ERR_ARG).  Launches kernel by kernel; no cudaMalloc, no graph capture, no event or
+ * stream creation. */
 int fdtdpic_run_noalloc(int precision, const FdtdInstance *h_inst, const FdtdInstance *d_inst,
                         const double *d_pml_tab, const double *d_src, void *d_state, void *d_probe,
                         const PicBeam *beam, int32_t *d_cell, void *d_frac, void *d_ux,
@@ -441,6 +444,65 @@ int fdtdpic_variant_check(int op, int n_rows, const FdtdVariantRow *h_rows, int6
 int fdtdpic_variant_run(int op, int precision, int n_rows, const FdtdVariantRow *h_rows,
                         const FdtdVariantRow *d_rows, int64_t stride, void *const *arrays,
                         fdtdpic_stream_t stream);
+
+/* ---- Per-step updates, one launch each ----------------------------------------------------
+ * The unit of work of the reference's module functions, for callers that build their own time
+ * loop from them.  Each operation updates cells [lo, hi) of FP64 device arrays (n elements
+ * each; arrays[i] is slot a<i>, NULL where the operation allows it) with the reference's
+ * arithmetic in its operation order.  Cells of a range are independent (a cell writes only its
+ * own elements and reads neighbours of arrays the operation does not write).
+ *
+ *   FDTD_OP_CURL       a0 = y (in/out), a1 = x, a2 = s (NULL: 1), a3 = j (NULL: 0),
+ *                      a4..a6 = factor arrays (NULL: the scalar fval[i]):
+ *                      y[k] = y[k]*s[k] + ((x[k+xa] - x[k+xb]) - j[k]) op0 f0 op1 f1 op2 f2,
+ *                      op_i by fmode[i]: 0 skip, 1 multiply, 2 divide (left to right).
+ *                      BaseFDTD11.ADE_ExUpdate (BaseFDTD11.py:664), ADE_HyUpdate (:641),
+ *                      ADE_DxUpdate (:751); BaseFDTD.ADE_ExUpdate (BaseFDTD.py:401),
+ *                      ADE_HyUpdate (:392), CPML_ExUpdate (:357), CPML_HyUpdate (:351),
+ *                      ADE_DxUpdate (:418, its Dx half).
+ *   FDTD_OP_PSI        a0 = psi (in/out), a1 = y (in/out), a2 = x, a3 = b, a4 = c, a5 = C:
+ *                      psi = b*psi + c*(x[k+xa] - x[k+xb]); y = y + C*psi (s[0] >= 0) or
+ *                      y - C*psi (s[0] < 0).  BaseFDTD11.CPML_Psi_e_Update (:365),
+ *                      CPML_Psi_m_Update (:382); BaseFDTD.CPML_Psi_e_Update (:334),
+ *                      CPML_Psi_m_Update (:342).
+ *   FDTD_OP_POL        a0 = y (out), a1 = p1, a2 = p2, a3 = x: y = (A p1 + B p2) + C x with
+ *                      s = (A, B, C).  BaseFDTD11.ADE_PolarisationCurrent_Ex (:610, p1 = y),
+ *                      BaseFDTD.ADE_PolarisationCurrent_Ex (:378, p1 = tempVarPol).
+ *   FDTD_OP_EXCREATE   a0 = y (out), a1 = u, a2 = v: y = (u - v) / s[0].  ADE_ExCreate
+ *                      (BaseFDTD11.py:713, BaseFDTD.py:413), BaseFDTD.ADE_DxUpdate's Ex half.
+ *   FDTD_OP_NONLIN_EX  a0 = y (out), a1 = Dx, a2 = Acubic: y = Dx / (s[0] + s[1] Acubic) with
+ *                      s = (permit_0 Re(sqrt(1.2)), permit_0 chi3Stat).  NonLinExUpdate (:859).
+ *   FDTD_OP_ACUBIC     a0 = Acubic (out), a1 = Dx, a2 = d (out; NULL: not written):
+ *                      d = -|Dx/s[0]|^2, Acubic = Re(CubicEquationSolver.solve(s[1], s[2],
+ *                      s[3], d)[0]) when |d| > 1e-8, else 0.  AcubicFinder (:803) with
+ *                      Nonlin_Eqn_Setup (:795) and Nonlin_Cubic_Solver (:824); s = (permit_0,
+ *                      cub, qua, one).
+ * Stencil offsets xa, xb lie in {-1, 0, 1}; every stencil read must stay inside [0, n). */
+#define FDTD_OP_CURL 0
+#define FDTD_OP_PSI 1
+#define FDTD_OP_POL 2
+#define FDTD_OP_EXCREATE 3
+#define FDTD_OP_NONLIN_EX 4
+#define FDTD_OP_ACUBIC 5
+#define FDTD_STEP_OP_ARRAYS 8
+
+typedef struct FdtdStepOp {
+    int32_t op;       /* FDTD_OP_* */
+    int32_t lo, hi;   /* cells [lo, hi) */
+    int32_t xa, xb;   /* stencil offsets (CURL, PSI) */
+    int32_t fmode[3]; /* CURL factors: 0 skip, 1 multiply, 2 divide */
+    double fval[3];   /* CURL scalar factors (used where the factor array is NULL) */
+    double s[4];      /* the operation's scalars */
+} FdtdStepOp;
+
+/* Like fdtdpic_instance_layout, for FdtdStepOp. */
+int fdtdpic_step_op_layout(int64_t *out, int n);
+/* Host-side check of an operation and its array slots (FDTDPIC_OK or FDTDPIC_ERR_ARG). */
+int fdtdpic_step_op_check(const FdtdStepOp *op, double *const *arrays, int64_t n);
+/* Run one operation (arrays: FDTD_STEP_OP_ARRAYS device pointers, a host array); asynchronous
+ * on the stream. */
+int fdtdpic_step_op(const FdtdStepOp *op, double *const *arrays, int64_t n,
+                    fdtdpic_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -26,9 +26,15 @@
 
 namespace fdtdpic {
 
+// The update coefficients in the state type.  The curl coefficients (ue, uh, their slab values
+// and dt/dz) also keep the part of their FP64 value that T drops (*_lo: 0 in FP64): in FP32 a
+// coefficient rounded once is the same error at every cell and every step, a wave speed off by
+// up to 2^-24 whose phase error grows with the distance a pulse travels (a few 1e-5 relative
+// after the thousands of steps of the benchmarked runs); mul_c multiplies by the pair.
 template <typename T>
 struct Scal {
     T ue, ue_slab, uh, uh_slab, dtdz, eps0, pa, pb, pc, e0r, e0chi;
+    T ue_lo, ue_slab_lo, uh_lo, uh_slab_lo, dtdz_lo;
 };
 
 template <typename T>
@@ -38,8 +44,18 @@ __device__ inline Scal<T> make_scal(const FdtdInstance &I)
     s.ue = (T)I.ue; s.ue_slab = (T)I.ue_slab; s.uh = (T)I.uh; s.uh_slab = (T)I.uh_slab;
     s.dtdz = (T)I.dtdz; s.eps0 = (T)I.eps0; s.pa = (T)I.pol_a; s.pb = (T)I.pol_b;
     s.pc = (T)I.pol_c; s.e0r = (T)I.nl_e0; s.e0chi = (T)I.nl_e0chi;
+    s.ue_lo = (T)(I.ue - (double)s.ue);
+    s.ue_slab_lo = (T)(I.ue_slab - (double)s.ue_slab);
+    s.uh_lo = (T)(I.uh - (double)s.uh);
+    s.uh_slab_lo = (T)(I.uh_slab - (double)s.uh_slab);
+    s.dtdz_lo = (T)(I.dtdz - (double)s.dtdz);
     return s;
 }
+
+// x times a curl coefficient (hi, lo): FP64 x * hi, the reference's product; FP32 the product
+// with the coefficient's FP64 value to ~48 bits, rounded once more than x * hi (unbiased).
+__device__ __forceinline__ double mul_c(double x, double hi, double) { return x * hi; }
+__device__ __forceinline__ float mul_c(float x, float hi, float lo) { return fmaf(x, lo, x * hi); }
 
 // PML table column of cell k, or -1.
 __device__ __forceinline__ int pml_col(const FdtdInstance &I, int k)
@@ -272,10 +288,12 @@ __device__ __forceinline__ void e_cell(const FdtdInstance &I, const Scal<T> &c, 
     }
     const int col = pml_col(I, k);
     const T den = (col >= 0) ? s.tab_at(FDTD_TAB_DENE, col) : T(1);
-    const T up = (I.mode == FDTD_MODE_FREESPACE && slab) ? c.ue_slab : c.ue;
+    const bool fs_slab = I.mode == FDTD_MODE_FREESPACE && slab;
+    const T up = fs_slab ? c.ue_slab : c.ue;
+    const T up_lo = fs_slab ? c.ue_slab_lo : c.ue_lo;
     T dh = hk - hkm;
     if (has_jx) dh = dh - jxv;
-    ex = ex + dh * up * den;
+    ex = ex + mul_c(dh, up, up_lo) * den;
     if ((I.cpml_lo && k < I.pml) || (I.cpml_hi && k >= n - I.pml)) {
         T &psi = s.PsiE(col, k);
         psi = s.tab_at(FDTD_TAB_BEX, col) * psi + s.tab_at(FDTD_TAB_CEX, col) * (hk - hkm);
@@ -290,7 +308,7 @@ __device__ __forceinline__ void e_cell(const FdtdInstance &I, const Scal<T> &c, 
         }
         T dhd = hk_d - hkm_d;
         if (dx_jx && has_jx) dhd = dhd - jxv;
-        const T dx = s.Dx(k) + dhd * c.dtdz * den;
+        const T dx = s.Dx(k) + mul_c(dhd, c.dtdz, c.dtdz_lo) * den;
         s.Dx(k) = dx;
         if (I.mode == FDTD_MODE_KERR) {
             const T A = kr.root(dx, c.eps0, nfb);
@@ -315,8 +333,10 @@ __device__ __forceinline__ void h_cell(const FdtdInstance &I, const Scal<T> &c, 
     const bool slab = (k >= I.front) && (k < I.rear);
     const int col = pml_col(I, k);
     const T den = (col >= 0) ? s.tab_at(FDTD_TAB_DENH, col) : T(1);
-    const T uh = (I.mode == FDTD_MODE_FREESPACE && slab) ? c.uh_slab : c.uh;
-    hy = hy + (exk1 - exk) * uh * den;
+    const bool fs_slab = I.mode == FDTD_MODE_FREESPACE && slab;
+    const T uh = fs_slab ? c.uh_slab : c.uh;
+    const T uh_lo = fs_slab ? c.uh_slab_lo : c.uh_lo;
+    hy = hy + mul_c(exk1 - exk, uh, uh_lo) * den;
     if ((I.cpml_lo && k < I.pml) || (I.cpml_hi && k >= n - I.pml && k < n - 1)) {
         T &psi = s.PsiH(col, k);
         psi = s.tab_at(FDTD_TAB_BMY, col) * psi + s.tab_at(FDTD_TAB_CMY, col) * (exk1 - exk);

@@ -15,9 +15,14 @@
 // word a run reads it first writes (the accumulators and bin counts are zeroed at the start of
 // the call).  On first use on a device the call looks up the array's device address
 // (cudaGetSymbolAddress with that device current) and keeps it; make that first call before any
-// stream capture.  The call allocates nothing: no cudaMalloc/cudaFree, no graph capture, no
-// event or stream creation.
+// stream capture.  The kept address belongs to the device's current context: a process that
+// calls cudaDeviceReset must not call this entry point on that device afterwards (the array is
+// reloaded at another address).  The call allocates nothing: no cudaMalloc/cudaFree, no graph
+// capture, no event or stream creation.  It takes the streaming kernels only: the persistent
+// tiled path (PicBeam.path mode 2) needs scratch sized per tile and is refused (ERR_ARG).
 #include <cuda_runtime.h>
+
+#include <mutex>
 
 #include "fdtdpic.h"
 #include "pic_kernel.cuh"
@@ -44,6 +49,7 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES]
 // Host-side device addresses of g_noalloc_scratch, one per device (the symbol's host name is
 // not a device address).
 void *g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+std::mutex g_noalloc_lock;  // first calls from several host threads look the address up once
 
 int noalloc_scratch(unsigned char **out)
 {
@@ -51,6 +57,7 @@ int noalloc_scratch(unsigned char **out)
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fdtdpic::cuda_status(e);
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return FDTDPIC_ERR_NODEV;
+    std::lock_guard<std::mutex> guard(g_noalloc_lock);
     if (!g_noalloc_ptr[dev]) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -82,6 +89,10 @@ extern "C" int fdtdpic_run_noalloc(int precision, const FdtdInstance *h_inst,
         return FDTDPIC_ERR_ARG;
     if (b.n_part > 0 && (!d_cell || !d_frac || !d_ux || !d_uz || !d_id)) return FDTDPIC_ERR_ARG;
     if (precision != FDTDPIC_F64 && precision != FDTDPIC_F32) return FDTDPIC_ERR_ARG;
+    // the path word as fdtdpic_run checks it; the tiled path (mode 2) is not available here
+    if ((b.path & ~(FDTDPIC_PATH_MODE | FDTDPIC_PATH_CELLS_INSIDE)) != 0 ||
+        (b.path & FDTDPIC_PATH_MODE) > 1)
+        return FDTDPIC_ERR_ARG;
     const int64_t need = fdtdpic_scratch_bytes(precision, h_inst->nz, b.n_part);
     if (need <= 0 || need > (int64_t)NOALLOC_SCRATCH_BYTES) return FDTDPIC_ERR_OOM;
     unsigned char *scr = nullptr;

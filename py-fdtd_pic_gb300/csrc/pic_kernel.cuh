@@ -448,11 +448,11 @@ __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
             const T jxk = Fix<T>::join(wx[u], a.jinv, a.jinv_f);
             const int kd = k >= 1 ? cell_kind(I, k) : CELL_GENERIC;
             if (kd == CELL_VACUUM) {
-                // e_cell: ex + ((hk - hkm) - jx) * ue * den, den = 1
-                s.ex[k] = ex[u] + ((hk[u] - hkm[u]) - jxk) * c.ue;
+                // e_cell: ex + mul_c((hk - hkm) - jx, ue) * den, den = 1
+                s.ex[k] = ex[u] + mul_c((hk[u] - hkm[u]) - jxk, c.ue, c.ue_lo);
             } else if (kd == CELL_KERR) {
-                // e_cell's slab branch: Dx + ((hk - hkm) - jx) * dtdz * den, the Kerr root, Ex
-                const T d = dx[u] + ((hk[u] - hkm[u]) - jxk) * c.dtdz;
+                // e_cell's slab branch: Dx + mul_c((hk - hkm) - jx, dtdz) * den, the Kerr root, Ex
+                const T d = dx[u] + mul_c((hk[u] - hkm[u]) - jxk, c.dtdz, c.dtdz_lo);
                 const T A = kr.root(d, c.eps0, &nfb);
                 if (a.last) gA[k] = A;
                 s.dx[k] = d;
@@ -517,9 +517,9 @@ __device__ __forceinline__ void pic_h_body(const PicField<T> &a, int t_arg, int 
             const int k = k0 + u * stride;
             if (k >= n - 1) break;
             if (cell_kind(I, k) != CELL_GENERIC) {
-                // h_cell: hy + (ex[k+1] - ex[k]) * uh * den with den = 1 (interior cells are
+                // h_cell: hy + mul_c(ex[k+1] - ex[k], uh) * den with den = 1 (interior cells are
                 // outside the slab or in a Kerr slab, so uh is the outside value)
-                s.hy[k] = hy[u] + (e1[u] - e0[u]) * c.uh;
+                s.hy[k] = hy[u] + mul_c(e1[u] - e0[u], c.uh, c.uh_lo);
             } else {
                 RegH<T> r{hy[u], e0[u], e1[u], cell_use(I, k).psih ? s.psih[k] : T(0), s.tab,
                           k, s.W};
@@ -544,16 +544,16 @@ __global__ void __launch_bounds__(256, 4) pic_h_kernel(PicField<T> a, int t_arg)
 // TF/SF correction and the free-space slab's coefficient remain.
 template <typename T>
 struct HOnTheFly {
-    T src_h, uh, uh_slab;
+    T src_h, uh, uh_slab, uh_lo, uh_slab_lo;
     int tfsf_cell, slab_lo, slab_hi;
-    int plain;  // no TF/SF cell and no slab coefficient: hy + (e1 - e0) * uh for every node
+    int plain;  // no TF/SF cell and no slab coefficient: hy + mul_c(e1 - e0, uh) for every node
 };
 template <typename T>
 __device__ __forceinline__ T h_on_the_fly(const HOnTheFly<T> &q, int k, T hy, T e0, T e1)
 {
     if (k == q.tfsf_cell) hy = hy - q.src_h;
-    const T uh = (k >= q.slab_lo && k < q.slab_hi) ? q.uh_slab : q.uh;
-    return hy + (e1 - e0) * uh;
+    const bool in = k >= q.slab_lo && k < q.slab_hi;
+    return hy + mul_c(e1 - e0, in ? q.uh_slab : q.uh, in ? q.uh_slab_lo : q.uh_lo);
 }
 
 // The register budget is the compiler's (40 in FP32): capping it at 32 for a full SM of push
@@ -600,6 +600,8 @@ __global__ void __launch_bounds__(PIC_THREADS, (FUSE_H && sizeof(T) == 4) ? 6 : 
             q.src_h = src_h_at<T>(I, hf.f.src, pic_step_index(hf, th));
             q.uh = hf.fc->c.uh;
             q.uh_slab = hf.fc->c.uh_slab;
+            q.uh_lo = hf.fc->c.uh_lo;
+            q.uh_slab_lo = hf.fc->c.uh_slab_lo;
             q.tfsf_cell = I.tfsf ? I.nzsrc - 1 : INT_MIN;
             const bool fs = I.mode == FDTD_MODE_FREESPACE;
             q.slab_lo = fs ? I.front : 0;
@@ -653,8 +655,8 @@ __global__ void __launch_bounds__(PIC_THREADS, (FUSE_H && sizeof(T) == 4) ? 6 : 
                 const HOnTheFly<T> &q = q_s;
                 T n0, n1;
                 if (q.plain) {  // the same operations as h_on_the_fly without its two terms
-                    n0 = p0 + (e1 - e0) * q.uh;
-                    n1 = p1 + (e2 - e1) * q.uh;
+                    n0 = p0 + mul_c(e1 - e0, q.uh, q.uh_lo);
+                    n1 = p1 + mul_c(e2 - e1, q.uh, q.uh_lo);
                 } else {
                     n0 = h_on_the_fly<T>(q, j, p0, e0, e1);
                     n1 = h_on_the_fly<T>(q, j + 1, p1, e1, e2);

@@ -33,6 +33,7 @@ UNITS = {
     "noalloc.cu": [],
     "setup.cu": ["-fmad=false"],  # set-up products and sums round one by one, as numpy's
     "variants.cu": ["-fmad=false"],  # the uncalled ADE variants, rounded as the reference's
+    "stepops.cu": ["-fmad=false"],  # per-step module functions, rounded as the reference's
 }
 
 

@@ -76,6 +76,29 @@ def beam_constants(dz, dt, weight, mu0, q=Q_E, m=M_E):
                 kJ=q * weight * C0, kJz=q * weight * dz / dt)
 
 
+@dataclass
+class PicSnapshot:
+    """Everything a :class:`PicRun` carries between calls, on the host (see PicRun.snapshot)."""
+    step_done: int
+    path: int
+    state: torch.Tensor
+    hyp: torch.Tensor
+    jx: torch.Tensor
+    jz: torch.Tensor
+    probe: torch.Tensor
+    status: torch.Tensor
+    cell: torch.Tensor
+    frac: torch.Tensor
+    ux: torch.Tensor
+    uz: torch.Tensor
+    id: torch.Tensor
+
+    def nbytes(self) -> int:
+        return sum(t.numel() * t.element_size() for t in (
+            self.state, self.hyp, self.jx, self.jz, self.probe, self.status, self.cell,
+            self.frac, self.ux, self.uz, self.id))
+
+
 class PicRun:
     """One grid plus a beam, resident on the GPU; ``step(n)`` advances n steps.
 
@@ -165,6 +188,63 @@ class PicRun:
         self.d_probe.zero_()
         self.d_status.zero_()
         self.step_done = 0
+
+    def snapshot(self) -> "PicSnapshot":
+        """Host copy of everything the run carries between calls: the grid state (Ex, Hy, Dx,
+        P, P one step back, both psi arrays, Acubic), Hy one half step back, the last grid
+        currents, the probe traces so far, the status words, the particles (in their current
+        order, with their ids) and the step reached.  The scratch holds nothing between calls
+        (the deposit accumulators are cleared by every step that reads them; the step counter
+        and the re-binning buffers are set by each call), so :meth:`restore` of this snapshot
+        into a run of the same grid and beam sizes continues exactly: bit for bit the run that
+        was never stopped.  Synchronises the device."""
+        torch.cuda.synchronize(self.dev)
+        cp = lambda t: t.to("cpu", copy=True)  # noqa: E731
+        return PicSnapshot(step_done=self.step_done, path=int(self.pb.path),
+                           state=cp(self.d_state), hyp=cp(self.d_hyp), jx=cp(self.d_jx),
+                           jz=cp(self.d_jz), probe=cp(self.d_probe), status=cp(self.d_status),
+                           cell=cp(self.d_cell), frac=cp(self.d_frac), ux=cp(self.d_ux),
+                           uz=cp(self.d_uz), id=cp(self.d_id))
+
+    def restore(self, snap: "PicSnapshot"):
+        """Load a snapshot taken from a run of the same grid and beam sizes and precision; the
+        next :meth:`step` continues from its step."""
+        pairs = ((self.d_state, snap.state), (self.d_hyp, snap.hyp), (self.d_jx, snap.jx),
+                 (self.d_jz, snap.jz), (self.d_probe, snap.probe), (self.d_status, snap.status),
+                 (self.d_cell, snap.cell), (self.d_frac, snap.frac), (self.d_ux, snap.ux),
+                 (self.d_uz, snap.uz), (self.d_id, snap.id))
+        for dst, src in pairs:
+            if dst.shape != src.shape or dst.dtype != src.dtype:
+                raise ValueError("snapshot of another grid, beam or precision: "
+                                 f"{tuple(src.shape)} {src.dtype} vs {tuple(dst.shape)} {dst.dtype}")
+        for dst, src in pairs:
+            dst.copy_(src)
+        self.pb.path = (self.pb.path & ~PATH_CELLS_INSIDE) | (snap.path & PATH_CELLS_INSIDE)
+        self.step_done = int(snap.step_done)
+
+    def run_host(self, cell, frac, ux, uz, n_steps=None, stream=None):
+        """One run from a beam in host memory: copy it in (pinned host tensors copy
+        asynchronously), start from zero fields, run ``n_steps`` (default: every step of the
+        grid) and return the probe traces and the final Ex as host tensors.  Particle ids are
+        the beam's indices."""
+        st = stream or torch.cuda.current_stream(self.dev)
+        c = torch.as_tensor(cell)
+        inside = c.numel() == 0 or (int(c.min()) >= self.beam.clo and int(c.max()) < self.beam.chi)
+        self.pb.path = self.path_mode | (PATH_CELLS_INSIDE if inside else 0)
+        with torch.cuda.stream(st):
+            for dst, src in ((self.d_cell, c), (self.d_frac, frac), (self.d_ux, ux),
+                             (self.d_uz, uz)):
+                dst.copy_(torch.as_tensor(src), non_blocking=True)
+            self.d_id.copy_(torch.arange(self.d_id.numel(), dtype=torch.int32,
+                                         device=self.dev), non_blocking=True)
+            self.d_hyp.zero_()
+            self.d_status.zero_()
+        self.step_done = 0
+        self.step(self.grid.n_steps if n_steps is None else n_steps, stream=st)
+        with torch.cuda.stream(st):
+            probes = self.d_probe.to("cpu", non_blocking=False)
+            ex = self.d_state[:self.grid.nz + 1].to("cpu", non_blocking=False)
+        return probes, ex
 
     def fields(self):
         n = self.grid.nz + 1

@@ -102,10 +102,15 @@ class Done:
     status: np.ndarray
     fields: dict | None = None
     particles: dict | None = None
+    error: str | None = None  # None: ran to completion with a clean status word
 
     @property
     def latency(self):
         return self.finished - self.arrival
+
+
+class _Rejected(ValueError):
+    """A request the library's slot check refused."""
 
 
 @dataclass
@@ -128,6 +133,7 @@ class _Active:
     cost_ns: float  # predicted ns per step for one CTA
     admitted: float
     outs: dict = field(default_factory=dict)
+    cancelled: bool = False
 
 
 class Server:
@@ -141,12 +147,18 @@ class Server:
     most max_big_busy while some do.  Each streaming run is latency-bound and holds few SMs, so
     several share an otherwise idle GPU (on GB300 the served stream's knee moved from 4 to 8 req/s
     going from 2 to 8 concurrent runs, 16 gained nothing), but under overload eight starved the
-    slot rounds (12.8 instead of ~200 req/s completed), hence the lower limit then."""
+    slot rounds (12.8 instead of ~200 req/s completed), hence the lower limit then.
+
+    Failures retire the request with ``Done.error`` set and leave the others untouched: a
+    request whose preparation raised ("prepare: ..."), one cancelled with :meth:`cancel`
+    ("cancelled"), one whose buffers could not be allocated while nothing else held memory
+    ("out of device memory"; with other requests resident it waits for them to retire and is
+    tried again), one whose kernel flagged a status bit ("status: ...")."""
 
     def __init__(self, precision="f32", hbm_budget=150e9, max_active=None, chunk_ms=3.0,
                  threads=512, smem_bytes=64 * 1024, max_inflight=2, keep_state=False,
                  max_admit_per_poll=64, prefetch=128, device=None, clock=time.perf_counter,
-                 big_ms=100.0, max_big=8, max_big_busy=2):
+                 big_ms=100.0, max_big=8, max_big_busy=2, fault_hook=None):
         _require_cuda()
         self.L = lib()
         check_slot_layout(self.L)
@@ -169,6 +181,12 @@ class Server:
         self.a_cell, self.a_cell_global, self.a_part = 2.5, 6.0, 4.0
         self.keep_state = keep_state
         self.clock = clock
+        # fault_hook(stage, req), if given, runs before a request's device buffers are
+        # allocated (stage "alloc"); an exception it raises is handled exactly as a failed
+        # allocation (tests inject out-of-memory this way, on the host)
+        self.fault_hook = fault_hook
+        self.cancelled: set = set()
+        self.oom_retries = 0
         # rounds on a high-priority stream; each streaming-kernel request on a low-priority
         # stream of its own (its set-up's copies then wait for nothing else)
         self.stream = torch.cuda.Stream(device=self.dev, priority=-1)
@@ -214,13 +232,11 @@ class Server:
 
     # ---- sizes and costs --------------------------------------------------------------------
     def request_bytes(self, req: Request) -> int:
-        ts = 8 if self.prec == F64 else 4
-        n = req.nz + 1
-        b = (STATE_ARRAYS * n * ts + 2 * req.n_steps * ts + 2 * req.n_steps * 8 +
-             8 * (2 * req.pml + 1) * 8)
-        if req.n_part:
-            b += req.n_part * (4 + 3 * ts) + 3 * n * ts + 2 * self.W * n * 8
-        return int(b) + 4096
+        return slot_request_bytes(self.prec, req.nz, req.n_steps, req.n_part, req.pml)
+
+    def big_request_bytes(self, req: Request) -> int:
+        return streaming_request_bytes(self.prec, req.nz, req.n_steps, req.n_part, req.pml,
+                                       self.L)
 
     def _step_cost_ns(self, g: Grid, n_part: int) -> float:
         resident = n_part == 0 and self._resident_bytes(g) <= self.smem
@@ -242,6 +258,19 @@ class Server:
     def submit(self, req: Request):
         self._unadmitted += 1
         self._inbox.put(req)
+
+    def cancel(self, rid: int):
+        """Cancel request ``rid``.  A request not yet admitted is dropped when it reaches
+        admission; one in a slot is retired after the rounds already enqueued for it (its
+        probes then hold the steps run so far); a streaming run already enqueued runs out and
+        its result is discarded.  Each is reported with ``error="cancelled"``."""
+        self.cancelled.add(rid)
+
+    def _fail(self, req: Request, now: float, error: str):
+        """Retire a request that never ran."""
+        self.done.append(Done(rid=req.rid, arrival=req.arrival, admitted=now, finished=now,
+                              probes=np.zeros((0, 2)), status=np.zeros(4, np.int32),
+                              error=error))
 
     def close(self):
         """Stop the preparation threads (pending requests are dropped) and wait for the work
@@ -332,15 +361,15 @@ class Server:
                 if not self._big_ready:
                     break
                 req = self._big_ready[0]
-                need = self.request_bytes(req)
-                if self.bytes_in_use + need > self.budget and (self.active or self.big):
+                need = self.big_request_bytes(req)
+                if not (req._error is not None or req.rid in self.cancelled or
+                        fits_budget(self.bytes_in_use, need, self.budget,
+                                    bool(self.active or self.big))):
                     break
                 self._big_ready.popleft()
                 self._ready_cv.notify_all()
-            self._unadmitted -= 1
-            if req._error is not None:
-                raise req._error
-            self._place_big(req, need, now)
+            if not self._admit_one(req, need, now, big=True):
+                break
             admitted += 1
         while self.free and admitted < self.max_admit:
             with self._ready_cv:
@@ -348,16 +377,45 @@ class Server:
                     break
                 req = self._ready[0]
                 need = self.request_bytes(req)
-                if self.bytes_in_use + need > self.budget and (self.active or self.big):
+                if not (req._error is not None or req.rid in self.cancelled or
+                        fits_budget(self.bytes_in_use, need, self.budget,
+                                    bool(self.active or self.big))):
                     break
                 self._ready.popleft()
                 self._ready_cv.notify_all()
-            self._unadmitted -= 1
-            if req._error is not None:
-                raise req._error
-            self._place(req, need, now)
+            if not self._admit_one(req, need, now, big=False):
+                break
             admitted += 1
         return admitted
+
+    def _admit_one(self, req: Request, need: int, now: float, big: bool) -> bool:
+        """Place one request taken off a ready queue.  False when its allocation failed while
+        other requests hold memory: it goes back to the head of its queue to wait for them."""
+        self._unadmitted -= 1
+        if req._error is not None:
+            self._fail(req, now, f"prepare: {type(req._error).__name__}: {req._error}")
+            return True
+        if req.rid in self.cancelled:
+            self.cancelled.discard(req.rid)
+            self._fail(req, now, "cancelled")
+            return True
+        try:
+            if self.fault_hook is not None:
+                self.fault_hook("alloc", req)
+            (self._place_big if big else self._place)(req, need, now)
+            return True
+        except _Rejected as e:
+            self._fail(req, now, str(e))
+            return True
+        except (torch.cuda.OutOfMemoryError, MemoryError) as e:
+            if self.active or self.big or self.inflight:
+                self.oom_retries += 1
+                self._unadmitted += 1
+                with self._ready_cv:
+                    (self._big_ready if big else self._ready).appendleft(req)
+                return False
+            self._fail(req, now, f"out of device memory: {e}")
+            return True
 
     def _place_big(self, req: Request, need: int, now: float):
         """Run a beam request on the streaming kernels, all its steps enqueued at once on a
@@ -372,7 +430,6 @@ class Server:
             run.step(g.n_steps, stream=st)
             ev = torch.cuda.Event()
             ev.record(st)
-        need += run.scratch_bytes
         self.bytes_in_use += need
         self.big.append(_Big(req=req, run=run, done_ev=ev, nbytes=need, admitted=now))
 
@@ -397,9 +454,13 @@ class Server:
                 fields = dict(Ex=f["Ex"], Hy=f["Hy"], Jx=jx, Jz=jz)
                 cell, frac, ux, uz = run.particles()
                 parts = dict(cell=cell, frac=frac, ux=ux, uz=uz)
+            cancelled = b.req.rid in self.cancelled
+            self.cancelled.discard(b.req.rid)
             self.done.append(Done(rid=b.req.rid, arrival=b.req.arrival, admitted=b.admitted,
                                   finished=self.clock(), probes=run.probes(), status=status,
-                                  fields=fields, particles=parts))
+                                  fields=None if cancelled else fields,
+                                  particles=None if cancelled else parts,
+                                  error="cancelled" if cancelled else status_error(status)))
             self.cell_steps += (g.nz + 1) * g.n_steps
             self.particle_steps += b.req.n_part * g.n_steps
             self.bytes_in_use -= b.nbytes
@@ -413,49 +474,52 @@ class Server:
         tdt, dev = self.tdt, self.dev
         n = g.nz + 1
         slot = self.free.pop()
-        with torch.cuda.stream(self.stream):
-            desc = host["desc"]
-            desc["step_begin"], desc["step_end"], desc["resume"] = 0, g.n_steps, 0
-            bufs = dict(table=host["table"].to(dev, non_blocking=True),
-                        src=host["src"].to(dev, non_blocking=True),
-                        state=torch.empty(host["n_state"], dtype=tdt, device=dev),
-                        probe=torch.zeros(host["n_probe"], dtype=tdt, device=dev))
-            s = self.slots_np[slot:slot + 1]  # a view: assignments land in the pinned table
-            s[...] = np.zeros(1, SLOT_DTYPE)
-            s["inst"] = desc
-            s["pml_tab"], s["src"] = bufs["table"].data_ptr(), bufs["src"].data_ptr()
-            s["state"], s["probe"] = bufs["state"].data_ptr(), bufs["probe"].data_ptr()
-            n_part = 0
-            if "cell" in host:
-                b = req.beam
-                n_part = b.n
-                bufs.update(cell=host["cell"].to(dev, non_blocking=True),
-                            frac=host["frac"].to(dev, non_blocking=True),
-                            ux=host["ux"].to(dev, non_blocking=True),
-                            uz=host["uz"].to(dev, non_blocking=True),
-                            hyp=torch.empty(n, dtype=tdt, device=dev),
-                            jx=torch.empty(n, dtype=tdt, device=dev),
-                            jz=torch.empty(n, dtype=tdt, device=dev),
-                            acc=torch.empty(2 * self.W * n, dtype=torch.int64, device=dev))
-                pb = PicBeam()
-                pb.n_part, pb.clo, pb.chi = b.n, b.clo, b.chi
-                consts = beam_constants(req.dz, req.dt, b.weight, req.mu0)
-                for k, v in consts.items():
-                    setattr(pb, k, v)
-                jscale = self.L.fdtdpic_pic_jscale(ctypes.byref(pb))
-                s["n_part"], s["clo"], s["chi"] = b.n, b.clo, b.chi
-                for k in ("cell", "frac", "ux", "uz", "hyp", "jx", "jz", "acc"):
-                    s[k] = bufs[k].data_ptr()
-                for k, v in consts.items():
-                    s[k] = v
-                s["jscale"] = jscale
-            rc = self.L.fdtdpic_slot_check(self.prec, s.ctypes.data)
-            if rc != 0:
-                self.free.append(slot)
-                raise ValueError(f"request {req.rid} rejected by fdtdpic_slot_check ({rc})")
-            sz = SLOT_DTYPE.itemsize
-            self.d_slots[slot * sz:(slot + 1) * sz].copy_(
-                self.h_slots[slot * sz:(slot + 1) * sz], non_blocking=True)
+        try:
+            with torch.cuda.stream(self.stream):
+                desc = host["desc"]
+                desc["step_begin"], desc["step_end"], desc["resume"] = 0, g.n_steps, 0
+                bufs = dict(table=host["table"].to(dev, non_blocking=True),
+                            src=host["src"].to(dev, non_blocking=True),
+                            state=torch.empty(host["n_state"], dtype=tdt, device=dev),
+                            probe=torch.zeros(host["n_probe"], dtype=tdt, device=dev))
+                s = self.slots_np[slot:slot + 1]  # a view: assignments land in the pinned table
+                s[...] = np.zeros(1, SLOT_DTYPE)
+                s["inst"] = desc
+                s["pml_tab"], s["src"] = bufs["table"].data_ptr(), bufs["src"].data_ptr()
+                s["state"], s["probe"] = bufs["state"].data_ptr(), bufs["probe"].data_ptr()
+                n_part = 0
+                if "cell" in host:
+                    b = req.beam
+                    n_part = b.n
+                    bufs.update(cell=host["cell"].to(dev, non_blocking=True),
+                                frac=host["frac"].to(dev, non_blocking=True),
+                                ux=host["ux"].to(dev, non_blocking=True),
+                                uz=host["uz"].to(dev, non_blocking=True),
+                                hyp=torch.empty(n, dtype=tdt, device=dev),
+                                jx=torch.empty(n, dtype=tdt, device=dev),
+                                jz=torch.empty(n, dtype=tdt, device=dev),
+                                acc=torch.empty(2 * self.W * n, dtype=torch.int64, device=dev))
+                    pb = PicBeam()
+                    pb.n_part, pb.clo, pb.chi = b.n, b.clo, b.chi
+                    consts = beam_constants(req.dz, req.dt, b.weight, req.mu0)
+                    for k, v in consts.items():
+                        setattr(pb, k, v)
+                    jscale = self.L.fdtdpic_pic_jscale(ctypes.byref(pb))
+                    s["n_part"], s["clo"], s["chi"] = b.n, b.clo, b.chi
+                    for k in ("cell", "frac", "ux", "uz", "hyp", "jx", "jz", "acc"):
+                        s[k] = bufs[k].data_ptr()
+                    for k, v in consts.items():
+                        s[k] = v
+                    s["jscale"] = jscale
+                rc = self.L.fdtdpic_slot_check(self.prec, s.ctypes.data)
+                if rc != 0:
+                    raise _Rejected(f"rejected by fdtdpic_slot_check ({rc})")
+                sz = SLOT_DTYPE.itemsize
+                self.d_slots[slot * sz:(slot + 1) * sz].copy_(
+                    self.h_slots[slot * sz:(slot + 1) * sz], non_blocking=True)
+        except BaseException:
+            self.free.append(slot)  # nothing of this request was handed to a round
+            raise
         req._host = None  # the staging copies are released once the copies have run
         self.bytes_in_use += need
         self.active[slot] = _Active(req=req, slot=slot, bufs=bufs, nbytes=need, next_step=0,
@@ -469,8 +533,14 @@ class Server:
         finishing = []
         pred_ns = 0.0
         work = [0.0, 0.0]  # cell-steps, particle-steps of this round
+        cancelled = []
         for slot, a in self.active.items():
             g = a.req.grid
+            if a.req.rid in self.cancelled:
+                # retired behind the rounds already enqueued for it; no new items
+                a.cancelled = True
+                cancelled.append(a)
+                continue
             if a.next_step >= g.n_steps:
                 continue
             k = max(1, int(self.chunk_ns / max(a.cost_ns, 1.0)))
@@ -483,7 +553,8 @@ class Server:
             a.next_step = t1
             if t1 >= g.n_steps:
                 finishing.append(a)
-        if not items:
+        finishing += cancelled
+        if not items and not cancelled:
             return False
         # longest items first: the queue then ends with short ones
         items.sort(key=lambda it: -self.active[it[0]].cost_ns * (it[2] - it[1]))
@@ -498,11 +569,12 @@ class Server:
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(self.stream)
-            check(self.L.fdtdpic_slots_run(
-                self.prec, ctypes.c_void_p(self.d_slots.data_ptr()), self.max_active,
-                ctypes.c_void_p(self._items_dev[r].data_ptr()), len(items),
-                ctypes.c_void_p(self.d_queue.data_ptr()), self.smem, self.threads, 0,
-                ctypes.c_void_p(self.stream.cuda_stream)), "fdtdpic_slots_run")
+            if items:
+                check(self.L.fdtdpic_slots_run(
+                    self.prec, ctypes.c_void_p(self.d_slots.data_ptr()), self.max_active,
+                    ctypes.c_void_p(self._items_dev[r].data_ptr()), len(items),
+                    ctypes.c_void_p(self.d_queue.data_ptr()), self.smem, self.threads, 0,
+                    ctypes.c_void_p(self.stream.cuda_stream)), "fdtdpic_slots_run")
             e1.record(self.stream)
             for a in finishing:
                 a.outs["probe"] = a.bufs["probe"].to("cpu", non_blocking=True)
@@ -518,8 +590,9 @@ class Server:
             done_ev.record(self.stream)
         for a in finishing:
             del self.active[a.slot]
+            self.cancelled.discard(a.req.rid)
         self.inflight.append((done_ev, e0, e1, finishing, pred_ns, len(items), work))
-        self.rounds += 1
+        self.rounds += 1 if items else 0
         return True
 
     def _complete(self, block=False):
@@ -553,10 +626,13 @@ class Server:
                                       Jz=a.outs["jz"].double().numpy())
                     if "cell" in a.outs:
                         parts = {k: a.outs[k].numpy() for k in ("cell", "frac", "ux", "uz")}
+                status = np.array(slot_rec["status"])
+                self.cancelled.discard(a.req.rid)  # a cancel that came after its last round
                 self.done.append(Done(
                     rid=a.req.rid, arrival=a.req.arrival, admitted=a.admitted, finished=now,
                     probes=a.outs["probe"].double().numpy().reshape(g.n_steps, 2),
-                    status=np.array(slot_rec["status"]), fields=fields, particles=parts))
+                    status=status, fields=fields, particles=parts,
+                    error="cancelled" if a.cancelled else status_error(status)))
                 self.bytes_in_use -= a.nbytes
                 self.free.append(a.slot)
                 a.bufs.clear()
@@ -640,6 +716,49 @@ class Server:
 # ------------------------------------------------------------------------------------------
 # the served request stream: Poisson arrivals, ragged grids, optional beams
 # ------------------------------------------------------------------------------------------
+def slot_request_bytes(prec: int, nz: int, n_steps: int, n_part: int, pml: int) -> int:
+    """Device bytes a request served in a slot holds: state, probes, sources, PML table and,
+    with a beam, its particles, Hy one half step back, the currents and the deposit
+    accumulators."""
+    ts = 8 if prec == F64 else 4
+    w = 2 if prec == F64 else 1
+    n = nz + 1
+    b = (STATE_ARRAYS * n * ts + 2 * n_steps * ts + 2 * n_steps * 8 + 8 * (2 * pml + 1) * 8)
+    if n_part:
+        b += n_part * (4 + 3 * ts) + 3 * n * ts + 2 * w * n * 8
+    return int(b) + 4096
+
+
+def streaming_request_bytes(prec: int, nz: int, n_steps: int, n_part: int, pml: int,
+                            L=None) -> int:
+    """Device bytes a request run on the streaming kernels holds: the slot form's buffers
+    plus particle ids, two more field-sized arrays and the streaming path's scratch
+    (fdtdpic_scratch_bytes: the re-binning copy of every particle array and the deposit
+    accumulators)."""
+    L = L or lib()
+    ts = 8 if prec == F64 else 4
+    scratch = int(L.fdtdpic_scratch_bytes(prec, int(nz), int(n_part)))
+    return (slot_request_bytes(prec, nz, n_steps, n_part, pml) + 4 * int(n_part) + scratch +
+            2 * (nz + 1) * ts)
+
+
+def fits_budget(in_use: int, need: int, budget: float, others_resident: bool) -> bool:
+    """Admission rule: a request is admitted when its bytes fit what the budget leaves, or
+    when nothing else is resident (a request larger than the whole budget still runs alone)."""
+    return in_use + need <= budget or not others_resident
+
+
+def status_error(status) -> str | None:
+    """The error a request's status word reports (include/fdtdpic.h FDTD_STATUS_*), or None."""
+    bits = int(status[1]) if len(status) > 1 else 0
+    what = [name for bit, name in ((1, "non-finite fields"), (2, "skipped"),
+                                   (4, "bounded wait gave up"), (8, "buffer overflow"))
+            if bits & bit]
+    if int(status[0]) > 0:
+        what.append(f"{int(status[0])} particles left the grid")
+    return ("status: " + ", ".join(what)) if what else None
+
+
 def streaming_limit(requests_waiting: bool, slots_free: bool, max_big: int,
                     max_big_busy: int) -> int:
     """How many streaming runs big requests may hold: several use an otherwise idle GPU well,

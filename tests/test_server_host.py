@@ -76,3 +76,34 @@ def test_streaming_limit_drops_while_requests_wait():
     assert streaming_limit(True, True, 8, 2) == 2
     assert streaming_limit(False, False, 8, 2) == 2
     assert streaming_limit(True, False, 8, 2) == 2
+
+
+def test_streaming_request_budget_counts_its_scratch():
+    """A 2M-particle request run on the streaming kernels holds its re-binning copies and
+    deposit accumulators besides its own buffers: admission counts them, so with other requests
+    resident a budget between the two totals refuses it."""
+    from fdtdpic._lib import lib
+    from fdtdpic.server import fits_budget, slot_request_bytes, streaming_request_bytes
+    L = lib()
+    nz, T, n_part = 65536, 50000, 2_000_000
+    for prec in (4, 8):
+        slot = slot_request_bytes(prec, nz, T, n_part, 20)
+        full = streaming_request_bytes(prec, nz, T, n_part, 20, L)
+        scratch = int(L.fdtdpic_scratch_bytes(prec, nz, n_part))
+        assert scratch >= n_part * (8 + 3 * prec)  # a second copy of every particle array
+        assert full >= slot + scratch
+        budget = (slot + full) // 2
+        assert fits_budget(0, slot, budget, True)
+        assert not fits_budget(0, full, budget, True)
+        # a request larger than the whole budget still runs when nothing else is resident
+        assert fits_budget(0, full, budget, False)
+        assert not fits_budget(budget - 10, 11, budget, True)
+
+
+def test_status_words_map_to_errors():
+    from fdtdpic.server import status_error
+    assert status_error(np.zeros(4, np.int32)) is None
+    assert status_error(np.array([0, 0, 7, 0])) is None  # FP64 cubic re-solves are no error
+    assert "non-finite" in status_error(np.array([0, 1, 0, 0]))
+    assert "bounded wait" in status_error(np.array([0, 4, 0, 0]))
+    assert "3 particles left" in status_error(np.array([3, 0, 0, 0]))

@@ -1,8 +1,9 @@
 """fdtdpic_run_noalloc: the beam + field step for callers that cannot allocate device memory
 (code inside another framework's memory pool, plug-ins in a host that reserved the device).
 
-It must give what fdtdpic_run gives with caller scratch, call after call (the compiled-in
-scratch array keeps the previous call's contents), and refuse runs larger than its 24 MiB.
+It must give what fdtdpic_run gives with caller scratch, bit for bit, call after call (the
+compiled-in scratch array keeps the previous call's contents), on the one-CTA field kernel and
+on the fused push-with-H launches, and refuse runs larger than its 24 MiB or on the tiled path.
 This file is collected last on purpose.
 """
 import ctypes
@@ -17,17 +18,21 @@ pytestmark = pytest.mark.gpu
 NZ, T, NPART = 512, 400, 20000
 DZ = 0.015
 DT = 0.5 * DZ / O.C0
+# (nz, clo, chi): a 512-cell grid (one-CTA field kernel) and a 1536-cell grid with the beam
+# inside its domain, whose push launches carry the previous step's H phase
+CASES = {"nz512": (512, 40, 480), "nz1536_fused": (1536, 40, 1480)}
 
 
-def _setup(precision):
+def _setup(precision, case="nz512"):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     import scipy.constants as sc
     from fdtdpic.grid import lorentz_kerr_grid
     from fdtdpic.pic import PicRun, make_beam
-    g = lorentz_kerr_grid(NZ, T, front=300, rear=400, nzsrc=60, probes=(50, 350), chi3=1e-2)
-    beam = make_beam(NPART, 40, 480, DZ)
+    nz, clo, chi = CASES[case]
+    g = lorentz_kerr_grid(nz, T, front=300, rear=400, nzsrc=60, probes=(50, 350), chi3=1e-2)
+    beam = make_beam(NPART, clo, chi, DZ)
     return torch, PicRun(g, beam, DZ, DT, sc.mu_0, precision=precision, sort_every=32)
 
 
@@ -63,24 +68,26 @@ def _snapshot(run):
                 parts=run.particles(), status=run.status().copy())
 
 
-def _compare(a, b, tol):
+def _compare(a, b):
+    """Both entry points run the same kernels with exact integer deposits: equal bits."""
     for k in ("Ex", "Hy", "Dx", "probes", "jx", "jz"):
-        assert O.rel_l2(a[k], b[k]) <= tol, k
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
     for x, y in zip(a["parts"], b["parts"]):
-        assert O.rel_l2(x, y) <= tol
+        np.testing.assert_array_equal(x, y)
     assert a["status"][0] == 0 and b["status"][0] == 0
 
 
-@pytest.mark.parametrize("precision,tol", [("f32", 1e-6), ("f64", 1e-12)])
-def test_noalloc_matches_scratch_entry_point_twice(precision, tol):
-    torch, run = _setup(precision)
+@pytest.mark.parametrize("case", sorted(CASES))
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_noalloc_matches_scratch_entry_point_twice(precision, case):
+    torch, run = _setup(precision, case)
     run.reset()
     run.step(T)
     want = _snapshot(run)
     first = _noalloc_run(run)
     second = _noalloc_run(run)
-    _compare(first, want, tol)
-    _compare(second, want, tol)
+    _compare(first, want)
+    _compare(second, want)
 
 
 def test_noalloc_rejects_runs_beyond_its_scratch():
@@ -97,3 +104,11 @@ def test_noalloc_rejects_runs_beyond_its_scratch():
         _ptr(run.d_frac), _ptr(run.d_ux), _ptr(run.d_uz), _ptr(run.d_id), _ptr(run.d_jx),
         _ptr(run.d_jz), _ptr(run.d_hyp), _ptr(run.d_status), None)
     assert rc == -2  # FDTDPIC_ERR_OOM, before anything is launched
+    pb = type(run.pb).from_buffer_copy(run.pb)
+    pb.path = 2  # the tiled path's scratch is not sized against the array
+    rc = run.L.fdtdpic_run_noalloc(
+        run.prec, d.ctypes.data, _ptr(run.d_desc), _ptr(run.d_table), _ptr(run.d_src),
+        _ptr(run.d_state), _ptr(run.d_probe), ctypes.byref(pb), _ptr(run.d_cell),
+        _ptr(run.d_frac), _ptr(run.d_ux), _ptr(run.d_uz), _ptr(run.d_id), _ptr(run.d_jx),
+        _ptr(run.d_jz), _ptr(run.d_hyp), _ptr(run.d_status), None)
+    assert rc == -1  # FDTDPIC_ERR_ARG
