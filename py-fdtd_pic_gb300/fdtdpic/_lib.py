@@ -198,6 +198,12 @@ def _declare(L):
     L.fdtdpic_slots_run.argtypes = [c_int, P, c_int, P, c_int, P, c_i64, c_int, c_int, P]
     L.fdtdpic_run_noalloc.restype = c_int
     L.fdtdpic_run_noalloc.argtypes = [c_int] + [P] * 17
+    L.fdtdpic_step_op_layout.restype = c_int
+    L.fdtdpic_step_op_layout.argtypes = [P, c_int]
+    L.fdtdpic_step_op_check.restype = c_int
+    L.fdtdpic_step_op_check.argtypes = [P, P, c_i64]
+    L.fdtdpic_step_op.restype = c_int
+    L.fdtdpic_step_op.argtypes = [P, P, c_i64, P]
     for name, argt in _EXTRA_DECLS.items():
         if hasattr(L, name):
             fn = getattr(L, name)
