@@ -51,19 +51,20 @@ def _peaks():
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling during the timed region, of the GPU this process runs on (named by
+    its UUID: under CUDA_VISIBLE_DEVICES the local ordinal is not nvidia-smi's index)."""
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index=0):
-        self.index = index
+    def __init__(self, device=0):
+        self.gpu_id = _gpu_id(device)
         self.proc = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                ["nvidia-smi", f"--id={self.gpu_id}", f"--query-gpu={self.Q}",
                  "--format=csv,noheader,nounits", "-lms", "200"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
@@ -97,7 +98,25 @@ class Clocks:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "gpu": self.gpu_id}
+
+
+def _gpu_id(device):
+    """nvidia-smi's name for a torch device: its UUID (GPU-...), else its PCI bus id, else the
+    ordinal."""
+    try:
+        import torch
+        props = torch.cuda.get_device_properties(device)
+        u = str(getattr(props, "uuid", "") or "")
+        if u:
+            return u if u.startswith("GPU-") else "GPU-" + u
+        bus = getattr(props, "pci_bus_id", None)
+        if bus is not None:
+            return (f"{int(getattr(props, 'pci_domain_id', 0)):08x}:{int(bus):02x}:"
+                    f"{int(getattr(props, 'pci_device_id', 0)):02x}.0")
+    except Exception:
+        pass
+    return str(device)
 
 
 def _setup(precision):
@@ -111,24 +130,43 @@ def _setup(precision):
     return grid, beam, run, dt
 
 
-def run_ours(args):
-    import numpy as np
+def _launch_shares(precision):
+    """Per-kernel shares of the headline run's GPU time from the committed ncu launch list of
+    this workload (profiles/fdtd_pic_nz4096_np1m_launch_list.json), or None."""
+    path = os.path.join(ROOT, "profiles", "fdtd_pic_nz4096_np1m_launch_list.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d[precision]
+    except Exception:
+        return None
+
+
+def l2_copy_gbs(dev, mib=32, reps=200):
+    """Device-to-device copy bandwidth of a buffer that stays in the 129 MB L2 (read + write
+    bytes per second), CUDA events around reps back-to-back copies after a warm-up."""
     import torch
+    n = (mib << 20) // 4
+    a = torch.ones(n, dtype=torch.float32, device=dev)
+    b = torch.empty_like(a)
+    for _ in range(20):
+        b.copy_(a)
+    e0, e1 = _events()
+    e0.record()
+    for _ in range(reps):
+        b.copy_(a)
+    e1.record()
+    e1.synchronize()
+    return 2 * a.numel() * 4 * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+
+def _headline(args, precision, steps, warmup, flush, world, local):
+    """One precision of the headline: device-resident runs (the line's value), runs through the
+    public host-buffer call (e2e), and the push launch's roofline."""
+    import torch
     dev = torch.device("cuda", torch.cuda.current_device())
-    from fdtdpic.pic import FdtdPicTiming
-
-    grid, beam, run, dt = _setup(args.precision)
-    # device-resident copy of the initial beam: each bench step restarts from it
+    grid, beam, run, dt = _setup(precision)
     init = [t.clone() for t in (run.d_cell, run.d_frac, run.d_ux, run.d_uz, run.d_id)]
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
     def reset_device():
         for dst, src in zip((run.d_cell, run.d_frac, run.d_ux, run.d_uz, run.d_id), init):
@@ -137,7 +175,7 @@ def run_ours(args):
         run.d_status.zero_()
         run.step_done = 0
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         reset_device()
         run.step(T)
     torch.cuda.synchronize()
@@ -150,12 +188,12 @@ def run_ours(args):
             dist.barrier()
 
     times = []
-    with Clocks(local) as clk:
+    with Clocks(dev) as clk:
         barrier()
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.fill_(1)  # > L2 (129 MB): nothing of the previous step stays cached
             reset_device()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0, e1 = _events()
             e0.record()
             run.step(T)
             e1.record()
@@ -169,74 +207,102 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     units = (NZ + NP) * T
-    value = units * world / (ms * 1e-3) / 1e6
 
-    # end to end through the public API: beam from pinned host memory, results read back
-    h = [t.cpu().pin_memory() for t in init]
-    e2e_times = []
-    h2d = sum(t.numel() * t.element_size() for t in h)
-    d2h = 0
-    for _ in range(max(1, min(args.steps, 3))):
+    # end to end through the public call: PicRun.run_host takes the beam from pinned host
+    # memory and returns the probe traces and the final Ex on the host
+    host = [t.cpu().pin_memory() for t in init[:4]]
+    h2d = sum(t.numel() * t.element_size() for t in host)
+    e2e_times, d2h = [], 0
+    for _ in range(max(1, min(steps, 3))):
         flush.fill_(1)
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0, e1 = _events()
         e0.record()
-        for dst, src in zip((run.d_cell, run.d_frac, run.d_ux, run.d_uz, run.d_id), h):
-            dst.copy_(src, non_blocking=True)
-        run.d_hyp.zero_()
-        run.step_done = 0
-        run.step(T)
-        probes = run.d_probe.to("cpu", non_blocking=False)
-        ex = run.d_state[:NZ + 1].to("cpu", non_blocking=False)
+        probes, ex = run.run_host(*host)
         e1.record()
         e1.synchronize()
         e2e_times.append(e0.elapsed_time(e1))
         d2h = probes.numel() * probes.element_size() + ex.numel() * ex.element_size()
     e2e_ms = statistics.median(e2e_times)
 
-    # per-kernel GPU time (CUDA events around every launch) for the roofline
+    # the push launch's time: its share of the run's GPU time in the committed ncu launch list
+    # of this workload, times this run's measured step time
+    from fdtdpic.pic import FdtdPicTiming
     reset_device()
     tm = FdtdPicTiming()
-    run.step(T, timing=tm)
+    run.step(64, timing=tm)  # which kernels this workload takes (path 3: push carries H)
     torch.cuda.synchronize()
-    tiled = tm.path == 2
-    if tiled:
-        # one persistent launch runs every step: its algorithmic bytes are all steps' particle
-        # and cell traffic
-        push_ms = tm.push_ms
-        achieved = (BYTES_PER_PARTICLE * NP + BYTES_PER_CELL * NZ) * T / (push_ms * 1e-3) / 1e9
+    fused = tm.path == 3
+    bpp = BYTES_PER_PARTICLE * (2 if precision == "f64" else 1)
+    kernel = ("pic_push_kernel<%s, FUSE_H>" % ("double" if precision == "f64" else "float")
+              if fused else "pic_push_kernel")
+    shares = _launch_shares(precision)
+    n_push = T  # one push launch per step (fused except after each re-binning)
+    if shares and "push" in shares:
+        per_launch = shares["push"] * ms / n_push
+        source = ("launch-list share %.3f (profiles/fdtd_pic_nz4096_np1m_launch_list.json) x "
+                  "this run's ms_per_step / %d push launches" % (shares["push"], n_push))
     else:
-        push_ms = tm.push_ms / T
-        achieved = BYTES_PER_PARTICLE * NP / (push_ms * 1e-3) / 1e9
+        per_launch, source = None, "no launch list committed for this precision"
     peak, peak_kind = _peaks()
-    # DRAM bytes per launch of the dominant kernel from one ncu capture of this command
-    # (profiles/<kernel>_traffic.json, written from the capture summarised beside it)
-    traffic = None
-    prof = os.path.join(ROOT, "profiles",
-                        ("pic_tiled_kernel" if tiled else "pic_push_kernel") + "_traffic.json")
-    if os.path.exists(prof):
+    roof = {"bound": "hbm", "kernel": kernel, "path": "streaming", "unit": "GB/s",
+            "peak": peak, "peak_source": peak_kind, "bytes_per_launch": bpp * NP,
+            "per_launch_ms": None if per_launch is None else round(per_launch, 5),
+            "per_launch_source": source, "achieved": None, "frac": None, "traffic": None}
+    if per_launch:
+        achieved = bpp * NP / (per_launch * 1e-3) / 1e9
+        roof.update(achieved=round(achieved, 1), frac=round(achieved / peak, 3))
+        l2 = l2_copy_gbs(dev)
+        roof.update(l2_gbs=round(l2, 1), l2_frac=round(achieved / l2, 3),
+                    l2_note="the beam (16 MiB in FP32) and fields stay in L2 between steps: "
+                            "l2_frac is achieved / a live L2-resident copy's bandwidth")
+    prof = os.path.join(ROOT, "profiles", "pic_push_kernel_traffic.json")
+    if os.path.exists(prof) and precision == "f32":
         try:
-            tj = json.load(open(prof))
-            # the tiled kernel's launch covers every step of the run; a push launch one step
-            if not tiled or int(tj.get("time_steps", T)) == T:
-                traffic = float(tj["dram_bytes_per_launch"])
+            roof["traffic"] = float(json.load(open(prof))["dram_bytes_per_launch"])
         except Exception:
-            traffic = None
+            pass
+    # our kernels per run (the beam lies inside its domain, so each push launch carries the
+    # previous step's H phase): push and E phase per step, a standalone H phase before each
+    # re-binning and at each block's end (every 32 steps), five re-binning kernels (histogram,
+    # three-launch scan, scatter) every 32 steps, the step counter's advance per 64-step graph
+    # block, and init, constants, step-counter set and finish per run
+    launches_per_run = 2 * T + 6 * (T // 32) + T // 64 + 4
+    return dict(ms=ms, value=units * world / (ms * 1e-3) / 1e6, clocks=clk.summary(),
+                e2e={"value": round(units * world / (e2e_ms * 1e-3) / 1e6, 1), "unit": UNIT,
+                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                     "ms_per_step": round(e2e_ms, 3),
+                     "call": "PicRun.run_host(cell, frac, ux, uz) from pinned host tensors"},
+                roofline=roof, launches=launches_per_run * steps, run=run)
 
+
+def run_ours(args):
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    h = _headline(args, args.precision, args.steps, args.warmup, flush, world, local)
+    h.pop("run")
+    f64 = None
+    if args.precision == "f32" and not args.no_f64:
+        f64 = _headline(args, "f64", max(3, min(args.steps, 3)), 3, flush, world, local)
+        f64.pop("run")
+        torch.cuda.empty_cache()
     if rank != 0:
         if world > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
         return None
-    # our kernels per run: tiled = init, bin, the persistent kernel, offsets, unbin, status;
-    # streaming (this beam lies inside its domain, so each push launch carries the previous
-    # step's H phase) = push and E phase per step, a standalone H phase before each re-binning
-    # and at each block's end (every 32 steps), five re-binning kernels (histogram, three-launch
-    # scan, scatter) every 32 steps, the step counter's advance per 64-step graph block, and
-    # init, constants, step-counter set and finish per run
-    launches_per_run = 6 if tiled else 2 * T + 6 * (T // 32) + T // 64 + 4
+    ms = h["ms"]
     out = {
-        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+        "metric": METRIC, "value": round(h["value"], 1), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if args.precision == "f32" else "f64", "data": "synthetic (seeded)",
@@ -246,25 +312,16 @@ def run_ours(args):
                    "parallelism": f"one instance per GPU x{world}"},
         "mcell_steps_per_s": round(NZ * T * world / (ms * 1e-3) / 1e6, 1),
         "mparticle_steps_per_s": round(NP * T * world / (ms * 1e-3) / 1e6, 1),
-        "e2e": {"value": round(units * world / (e2e_ms * 1e-3) / 1e6, 1), "unit": UNIT,
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": round(e2e_ms, 3)},
-        "roofline": {"bound": "hbm",
-                     "kernel": ("pic_tiled_kernel<float>" if tiled else
-                                "pic_push_kernel<float, FUSE_H> (with the previous step's H phase)"
-                                if tm.path == 3 else "pic_push_kernel<float>"),
-                     "path": "tiled" if tiled else "streaming",
-                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 3), "peak_source": peak_kind,
-                     "traffic": traffic,
-                     "per_launch_ms": round(push_ms, 5),
-                     "bytes_per_launch": ((BYTES_PER_PARTICLE * NP + BYTES_PER_CELL * NZ) * T
-                                          if tiled else BYTES_PER_PARTICLE * NP),
-                     "kernel_share": {"push": round(tm.push_ms, 2), "field": round(tm.field_ms, 2),
-                                      "sort": round(tm.sort_ms, 2)}},
-        "gpu_launches": launches_per_run * args.steps,
-        "clocks": clk.summary(),
+        "e2e": h["e2e"], "roofline": h["roofline"], "gpu_launches": h["launches"],
+        "clocks": h["clocks"],
     }
+    if f64 is not None:
+        out["f64"] = {"dtype": "f64", "value": round(f64["value"], 1), "unit": UNIT,
+                      "steps": max(3, min(args.steps, 3)), "warmup": 3,
+                      "ms_per_step": round(f64["ms"], 3), "e2e": f64["e2e"],
+                      "roofline": f64["roofline"], "clocks": f64["clocks"],
+                      "note": "the same workload in FP64 on the GPU, beside the FP64 CPU "
+                              "reference arm"}
     for name, fn in (("sweep", bench_sweep), ("serve", bench_serve), ("knee", bench_serve_knee),
                      ("large", bench_large), ("variants", bench_variants)):
         if name in args.extra:
@@ -339,6 +396,8 @@ def bench_sweep(args, flush):
     status = sw.packed.d_status.cpu().numpy()
     fallbacks = int(sw.packed.d_fallbacks.cpu().numpy().sum())
     plain_rate, plain_ms = sweep.plain_per_instance_rate(grids, max_instances=16)
+    global_rate, _ = sweep.plain_global_rate(grids, max_instances=4)
+    best_plain = max(plain_rate, global_rate)
     batched = cells / ((fields_ms + spectra_ms) * 1e-3)
     dft_flops = 2.0 * (2 * sw.n) * (2 * sw.F) * sw.S  # real GEMM [2n x S] x [S x 2F]
     return {"workload": "sweep_4096inst_nz500-8000_steps8192_kerr_f32",
@@ -346,14 +405,17 @@ def bench_sweep(args, flush):
             "fields_ms": round(fields_ms, 2), "spectra_ms": round(spectra_ms, 2),
             "mcell_steps_per_s": round(batched / 1e6, 1),
             "plain_mcell_steps_per_s": round(plain_rate / 1e6, 1),
-            "vs_plain": round(batched / plain_rate, 1),
+            "plain_global_mcell_steps_per_s": round(global_rate / 1e6, 1),
+            "vs_plain": round(batched / best_plain, 1),
             "dft": "tcgen05 split-BF16x3, FP32 chunk sums, FP64 across chunks",
             "dft_gemm_tflops": round(dft_flops / (spectra_ms * 1e-3) / 1e12, 2),
             "dft_tensor_tflops": round(3 * dft_flops / (spectra_ms * 1e-3) / 1e12, 2),
             "dft_cuda_core_ms": round(min(c_ms), 2), "dft_tc_error": sw.dft_error(),
             "fp64_cubic_resolves": fallbacks, "bad_status": int((status != 0).sum()),
             "setup_s": {"host": round(setup_host_s, 3), "device": round(setup_device_s, 3)},
-            "plain": "same resident kernel, one instance per launch, 16 instances in sequence"}
+            "plain": "the better of two one-instance-per-launch forms: the resident kernel with "
+                     "one CTA (16 instances in sequence) and the global-memory path over every "
+                     "SM (fdtd1d_run_global, 4 instances in sequence)"}
 
 
 def bench_serve(args, flush):
@@ -579,7 +641,8 @@ def main():
     ap.add_argument("--extra", default="sweep,serve,knee,large,variants",
                     help="comma-separated extra sections: sweep, serve, knee, large, variants "
                          "('' for none)")
-    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--no-f64", action="store_true", help="skip the FP64 run of the headline")
     ap.add_argument("--knee-rates", default="1,2,4,8,16",
                     help="offered request rates (per second) of the serving knee section")
     ap.add_argument("--knee-seconds", type=float, default=8.0)

@@ -254,6 +254,29 @@ def plain_per_instance_rate(grids, precision="f32", threads=256, max_instances=3
     return cells / (e0.elapsed_time(e1) * 1e-3), e0.elapsed_time(e1)
 
 
+def plain_global_rate(grids, precision="f32", max_instances=4):
+    """Cell-steps/s of the other plain form: each instance alone on the global-memory path
+    (fdtd1d_run_global, fields in HBM, an E and an H launch per step over every SM), one
+    instance after another, on up to max_instances of the batch."""
+    sub = grids[:max_instances]
+    singles = []
+    for g in sub:
+        s = engine.upload([g], precision)
+        s.global_idx, s.resident = [0], []
+        singles.append(s)
+    st = torch.cuda.current_stream()
+    engine.launch(singles[0], stream=st)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for s in singles:
+        engine.launch(s, stream=st)
+    e1.record()
+    e1.synchronize()
+    cells = sum((g.nz + 1) * g.n_steps for g in sub)
+    return cells / (e0.elapsed_time(e1) * 1e-3), e0.elapsed_time(e1)
+
+
 # ------------------------------------------------------------------------------------------
 # autotuner: CTA size and grid for the resident batch kernel, cached per device and bucket
 # ------------------------------------------------------------------------------------------

@@ -20,10 +20,10 @@ runnable without changing a line of it:
   (``CubicEquationSolver.py:29``), so ``CubicSolver`` packs its four arguments and ``solve``
   unpacks them.  Nothing else in the reference is patched.
 
-Run from the repository root:  ``python tests/golden/make_golden.py`` (about two minutes;
-``python tests/golden/make_golden.py variants`` writes ``variants.npz`` alone;
-``python tests/golden/make_golden.py time`` times the reference's own Kerr integrator instead).
-It reads the reference from ``/root/reference`` (or ``$PYFDTD_REFERENCE``) and writes
+Run from the repository root with the reference checkout named by ``PYFDTD_REFERENCE``:
+``PYFDTD_REFERENCE=<checkout> python tests/golden/make_golden.py`` (about two minutes;
+a mode argument writes one fixture alone: ``variants`` -> ``variants.npz``, ``stepops`` ->
+``stepops.npz``; ``time`` times the reference's own Kerr integrator instead).  It writes
 ``*.npz`` beside this file.  The fixtures are committed; tests only read them.
 """
 from __future__ import annotations
@@ -41,7 +41,7 @@ import numpy as np
 import scipy
 import scipy.constants
 
-REF = os.environ.get("PYFDTD_REFERENCE", "/root/reference")
+REF = os.environ.get("PYFDTD_REFERENCE")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 sys.dont_write_bytecode = True
@@ -131,8 +131,10 @@ def _install_stubs():
     mpl = types.ModuleType("matplotlib")
     pylab = types.ModuleType("matplotlib.pylab")
     pyplot = types.ModuleType("matplotlib.pyplot")
-    mpl.pylab, mpl.pyplot = pylab, pyplot
-    sys.modules.update({"matplotlib": mpl, "matplotlib.pylab": pylab, "matplotlib.pyplot": pyplot})
+    animation = types.ModuleType("matplotlib.animation")
+    mpl.pylab, mpl.pyplot, mpl.animation = pylab, pyplot, animation
+    sys.modules.update({"matplotlib": mpl, "matplotlib.pylab": pylab, "matplotlib.pyplot": pyplot,
+                        "matplotlib.animation": animation})
     sys.modules["pyttsx3"] = types.ModuleType("pyttsx3")
 
     tests_pkg = types.ModuleType("Tests")
@@ -425,6 +427,147 @@ def variant_cases(mods):
     return out
 
 
+# arrays of Variables / CPML_Variables that the per-step functions read or write
+_V_ARRAYS = ("Ex", "Hy", "Dx", "Jx", "polarisationCurr", "tempVarPol", "tempTempVarPol",
+             "tempVarE", "tempTempVarE", "Acubic", "UpExMat", "UpHyMat", "UpExSelf", "UpHySelf",
+             "UpExHcompsCo", "UpHyEcompsCo")
+_CV_ARRAYS = ("psi_Ex", "psi_Hy", "beX", "ceX", "bmY", "cmY", "Cb", "C2", "den_Exdz",
+              "den_Hydz", "kappa_Ex", "kappa_Hy", "sigma_Ex", "sigma_Hy", "alpha_Ex", "alpha_Hy",
+              "eLoss_CPML", "mLoss_CPML", "Ca", "Cc", "C1", "C3")
+
+
+def stepop_cases(mods):
+    """The per-step functions of BaseFDTD11 that the integrators call (and the set-up chain of
+    boundCondManager), and the legacy BaseFDTD module's functions: each called once on seeded
+    state, recorded as ``<module>_<function>_<array>`` for every array it changed, with the
+    state it started from as ``<module>_in_<array>`` (every function starts from that state)."""
+    import BaseFDTD as B0
+    Variables, Params, CPML_Params, CPML_Variables = mods["classes"]
+    B11 = mods["B11"]
+    rng = np.random.Generator(np.random.PCG64(20261205))
+    out = {}
+    for tag, mod in (("b11", B11), ("b0", B0)):
+        P = make_params(Params, Nz=300, steps=64, dz=0.015, sc=0.5, front=100, rear=200, pml=20,
+                        nzsrc=60, x1=30, x2=270, freq_in=1e9)
+        P.nonLinMed, P.FreeSpace, P.TFSF = True, False, False
+        P.epsRe, P.muRe = 2.0, 1.0
+        P.eHcompsCo, P.eSelfCo, P.hEcompsCo, P.hSelfCo = 0.8, 0.99, 1.1, 0.98
+        V = Variables(P.Nz, P.timeSteps, P.vidInterval, 1)
+        lorentz(V, 2.0, 1.5e9, 2 * np.pi * 0.1e9)
+        V.chi3Stat = 1e-2
+        C_P = CPML_Params(P.dz)
+        C_V = CPML_Variables(P.Nz, P.timeSteps)
+        with contextlib.redirect_stdout(io.StringIO()):
+            mod.FieldInit(V, P)
+            V.UpHyMat, V.UpExMat = mod.EmptySpaceCalc(V, P)
+            if tag == "b0":
+                V.epsilon, V.mu, *_ = mod.Material(V, P)
+                UpHy, UpEx = mod.UpdateCoef(V, P)
+                out.update(b0_UpdateCoef_UpHyMat=np.asarray(UpHy).copy(),
+                           b0_UpdateCoef_UpExMat=np.asarray(UpEx).copy(),
+                           b0_Material_UpExSelf=V.UpExSelf.copy(),
+                           b0_Material_UpHySelf=V.UpHySelf.copy(),
+                           b0_Material_UpExHcompsCo=V.UpExHcompsCo.copy(),
+                           b0_Material_UpHyEcompsCo=V.UpHyEcompsCo.copy(),
+                           b0_EmptySpaceCalc_UpExMat=V.UpExMat.copy(),
+                           b0_EmptySpaceCalc_UpHyMat=V.UpHyMat.copy())
+                Exs, Hys = mod.SmoothTurnOn(V, P)
+                out.update(b0_SmoothTurnOn_Exs=np.asarray(Exs, float).copy(),
+                           b0_SmoothTurnOn_Hys=np.asarray(Hys, float).copy())
+            mod.CPML_FieldInit(V, P, C_V, C_P)
+            # the set-up chain in boundCondManager's order, each function's arrays recorded
+            for fn in ("CPML_ScalingCalc", "CPML_Ex_RC_Define", "CPML_HY_RC_Define",
+                       "CPML_Ex_Update_Coef", "CPML_Hy_Update_Coef", "denominators"):
+                getattr(mod, fn)(V, P, C_V, C_P)
+                for a in _CV_ARRAYS:
+                    out[f"{tag}_{fn}_{a}"] = np.asarray(getattr(C_V, a), float).copy()
+        scal = dict(Nz=P.Nz, pmlWidth=P.pmlWidth, materialFrontEdge=P.materialFrontEdge,
+                    materialRearEdge=P.materialRearEdge, nzsrc=P.nzsrc, delT=P.delT, dz=P.dz,
+                    permit_0=P.permit_0, permea_0=P.permea_0, courantNo=P.courantNo,
+                    CharImp=P.CharImp, freq_in=P.freq_in, c0=P.c0, epsRe=P.epsRe, muRe=P.muRe,
+                    eHcompsCo=P.eHcompsCo, eSelfCo=P.eSelfCo, hEcompsCo=P.hEcompsCo,
+                    hSelfCo=P.hSelfCo, kappaMax=C_P.kappaMax, sigmaOpt=C_P.sigmaOpt,
+                    alphaMax=C_P.alphaMax, r_scale=C_P.r_scale, r_a_scale=C_P.r_a_scale,
+                    plasmaFreqE=V.plasmaFreqE, omega_0E=V.omega_0E, gammaE=V.gammaE,
+                    chi3Stat=V.chi3Stat, alpha3=V.alpha3)
+        for k, v in scal.items():
+            out[f"{tag}_scal_{k}"] = v
+        # seeded state (fields of unit scale, Dx so that about half the slab passes the cubic's
+        # |d| > 1e-8 gate), recorded as the start of every per-step call
+        n = P.Nz + 1
+        e0 = P.permit_0
+        state = dict(Ex=rng.standard_normal(n), Hy=rng.standard_normal(n) / 377.0,
+                     Dx=e0 * 1e-4 * rng.standard_normal(n) * (rng.random(n) < 0.5) +
+                     e0 * 1e-5 * rng.standard_normal(n),
+                     Jx=1e-3 * rng.standard_normal(n), polarisationCurr=e0 * rng.standard_normal(n),
+                     tempVarPol=e0 * rng.standard_normal(n),
+                     tempTempVarPol=e0 * rng.standard_normal(n),
+                     tempVarE=rng.standard_normal(n), tempTempVarE=rng.standard_normal(n),
+                     Acubic=1e-3 * rng.random(n), UpHySelf=1 + 0.01 * rng.standard_normal(n),
+                     UpExSelf=1 + 0.01 * rng.standard_normal(n),
+                     psi_Ex=1e-3 * rng.standard_normal(n), psi_Hy=1e-3 * rng.standard_normal(n))
+        for k, v in state.items():
+            out[f"{tag}_in_{k}"] = v.copy()
+        for k in ("UpExMat", "UpHyMat", "UpExHcompsCo", "UpHyEcompsCo"):
+            out[f"{tag}_in_{k}"] = np.asarray(getattr(V, k), float).copy()
+        for k in _CV_ARRAYS:
+            if k not in state:
+                out[f"{tag}_in_{k}"] = np.asarray(getattr(C_V, k), float).copy()
+
+        def fresh():
+            for k in _V_ARRAYS:
+                src = out.get(f"{tag}_in_{k}")
+                if src is not None:
+                    setattr(V, k, src.copy())
+            for k in _CV_ARRAYS:
+                src = out.get(f"{tag}_in_{k}")
+                if src is not None:
+                    setattr(C_V, k, src.copy())
+
+        if tag == "b11":
+            calls = [("ADE_ExUpdate", lambda: mod.ADE_ExUpdate(V, P, C_V, C_P, 0)),
+                     ("CPML_Psi_e_Update", lambda: mod.CPML_Psi_e_Update(V, P, C_V, C_P)),
+                     ("CPML_Psi_m_Update", lambda: mod.CPML_Psi_m_Update(V, P, C_V, C_P)),
+                     ("ADE_DxUpdate", lambda: mod.ADE_DxUpdate(V, P, C_V, C_P)),
+                     ("AcubicFinder", lambda: mod.AcubicFinder(V, P)),
+                     ("NonLinExUpdate", lambda: mod.NonLinExUpdate(V, P)),
+                     ("ADE_HyUpdate", lambda: mod.ADE_HyUpdate(V, P, C_V, C_P)),
+                     ("ADE_PolarisationCurrent_Ex",
+                      lambda: mod.ADE_PolarisationCurrent_Ex(V, P, C_V, C_P, 0)),
+                     ("ADE_ExCreate", lambda: mod.ADE_ExCreate(V, P, C_V, C_P)),
+                     ("ADE_TempPolCurr", lambda: mod.ADE_TempPolCurr(V, P, C_V, C_P))]
+        else:
+            calls = [("CPML_Psi_e_Update", lambda: mod.CPML_Psi_e_Update(V, P, C_V, C_P)),
+                     ("CPML_Psi_m_Update", lambda: mod.CPML_Psi_m_Update(V, P, C_V, C_P)),
+                     ("CPML_HyUpdate", lambda: mod.CPML_HyUpdate(V, P, C_V, C_P)),
+                     ("CPML_ExUpdate", lambda: mod.CPML_ExUpdate(V, P, C_V, C_P)),
+                     ("ADE_TempPolCurr", lambda: mod.ADE_TempPolCurr(V, P)),
+                     ("ADE_PolarisationCurrent_Ex",
+                      lambda: mod.ADE_PolarisationCurrent_Ex(V, P, C_V, C_P)),
+                     ("ADE_HyUpdate", lambda: mod.ADE_HyUpdate(V, P, C_V, C_P)),
+                     ("ADE_ExUpdate", lambda: mod.ADE_ExUpdate(V, P, C_V, C_P)),
+                     ("ADE_ExCreate", lambda: mod.ADE_ExCreate(V, P, C_V, C_P)),
+                     ("ADE_DxUpdate", lambda: mod.ADE_DxUpdate(V, P, C_V, C_P))]
+        for fn, call in calls:
+            fresh()
+            with contextlib.redirect_stdout(io.StringIO()), warnings.catch_warnings():
+                warnings.simplefilter("ignore")
+                call()
+            for k in _V_ARRAYS:
+                a = np.asarray(getattr(V, k), float)
+                src = out.get(f"{tag}_in_{k}")
+                if src is not None and not np.array_equal(a, src):
+                    out[f"{tag}_{fn}_{k}"] = a.copy()
+            for k in _CV_ARRAYS:
+                a = np.asarray(getattr(C_V, k), float)
+                src = out.get(f"{tag}_in_{k}")
+                if src is not None and not np.array_equal(a, src):
+                    out[f"{tag}_{fn}_{k}"] = a.copy()
+            if fn == "AcubicFinder":
+                out["b11_AcubicFinder_cubPoly"] = np.asarray(V.cubPoly).copy()
+    return out
+
+
 def _no_debugger(*args, **kwargs):
     raise RuntimeError("the reference reached breakpoint() (a state its checks stop on)")
 
@@ -452,6 +595,8 @@ def time_reference(mods, n_steps=1024):
 
 
 def main(only=None):
+    if not REF or not os.path.isdir(REF):
+        sys.exit("set PYFDTD_REFERENCE to the reference checkout (fraserac/Py-FDTD_PIC)")
     sys.breakpointhook = _no_debugger
     raw_solve = _install_stubs()
     import BaseFDTD11 as B11
@@ -464,6 +609,11 @@ def main(only=None):
     meta = dict(numpy=np.__version__, scipy=scipy.__version__,
                 eps0=scipy.constants.epsilon_0, mu0=scipy.constants.mu_0)
 
+    if only == "stepops" or only is None:
+        np.savez_compressed(os.path.join(OUT, "stepops.npz"), **stepop_cases(mods), **meta)
+        print("stepops done", flush=True)
+        if only == "stepops":
+            return
     if only == "variants" or only is None:
         np.savez_compressed(os.path.join(OUT, "variants.npz"), **variant_cases(mods), **meta)
         print("variants done", flush=True)
