@@ -445,6 +445,26 @@ int fdtdpic_variant_run(int op, int precision, int n_rows, const FdtdVariantRow 
                         const FdtdVariantRow *d_rows, int64_t stride, void *const *arrays,
                         fdtdpic_stream_t stream);
 
+/* ---- Bounded waits ----------------------------------------------------------------------
+ * The persistent tiled PIC kernel's waits on its neighbours give up at a per-run deadline
+ * (default 20 s plus 1 ms per step) and the tensor-core DFT's mbarrier waits after a poll
+ * limit; a wait that gives up reports FDTDPIC_ERR_TIMEOUT (the tiled run's status word gets
+ * FDTD_STATUS_TIMEOUT, the DFT's d_err is set) and its kernel returns, so the context stays
+ * usable.  No counterpart in the reference, whose only failure handling is print + sys.exit
+ * (Environment_Setup.py:59-155) and breakpoint() (BaseFDTD11.py:535-537). */
+/* Set the tiled kernel's per-run deadline in nanoseconds for the runs launched after this call
+ * (0: the default).  Process-wide; meant for tests that make a run's waits run out (a wait
+ * that starts after the deadline gives up at once). */
+int fdtdpic_set_run_deadline(int64_t ns);
+/* One thread waits on something nothing completes and must give up.  which = 0: the tiled
+ * kernel's neighbour-flag wait on a flag nothing raises, deadline `limit` ns (<= 2e9) from its
+ * start (d_scratch: 2 int32 of device scratch, the flag and the abort word); which = 1: the
+ * DFT's mbarrier wait on a barrier nothing arrives on, `limit` polls (<= 2^26; d_scratch
+ * unused).  d_out (2 int32, device): [0] the code the wait reported (FDTDPIC_ERR_TIMEOUT when it
+ * gave up), [1] microseconds it waited. */
+int fdtdpic_wait_selftest(int which, int64_t limit, int32_t *d_out, int32_t *d_scratch,
+                          fdtdpic_stream_t stream);
+
 /* ---- Per-step updates, one launch each ----------------------------------------------------
  * The unit of work of the reference's module functions, for callers that build their own time
  * loop from them.  Each operation updates cells [lo, hi) of FP64 device arrays (n elements

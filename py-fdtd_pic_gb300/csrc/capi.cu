@@ -8,7 +8,13 @@
 #include "pic_kernel.cuh"
 #include "pic_tiled.cuh"
 
+#include <atomic>
+
 namespace fdtdpic {
+
+static std::atomic<long long> g_tiled_deadline_ns{0};
+
+long long tiled_deadline_override_ns() { return g_tiled_deadline_ns.load(); }
 
 int cuda_status(cudaError_t e)
 {
@@ -323,3 +329,10 @@ int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d
 }
 
 }  // extern "C"
+
+extern "C" int fdtdpic_set_run_deadline(int64_t ns)
+{
+    if (ns < 0) return FDTDPIC_ERR_ARG;
+    fdtdpic::g_tiled_deadline_ns.store((long long)ns);
+    return FDTDPIC_OK;
+}

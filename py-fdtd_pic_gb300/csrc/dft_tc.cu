@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "mbar_wait.cuh"
 #include "fdtdpic.h"
 
 namespace fdtdpic {
@@ -45,7 +46,6 @@ constexpr uint32_t TC_B_BLOCK = 2 * TC_B_HALF;
 constexpr uint32_t TC_STAGE = TC_A_BLOCK + TC_B_BLOCK;     // 48 KiB
 constexpr uint32_t TC_ACC_BYTES = TC_M * TC_N * 8;         // FP64 tile, 64 KiB
 constexpr uint32_t TC_SMEM = 2 * TC_STAGE + TC_ACC_BYTES + 64;
-constexpr long long TC_WAIT_LIMIT = 1LL << 26;             // mbarrier polls before giving up
 
 // Byte offset of element (row, k) of a K-major operand tile in the core-matrix layout.
 __host__ __device__ __forceinline__ uint32_t tc_off(int row, int k)
@@ -77,26 +77,6 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t da, uint64_t db
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
         "l"(da), "l"(db), "r"(TC_IDESC), "r"(acc));
-}
-
-__device__ __forceinline__ uint32_t tc_try_wait(uint32_t bar, uint32_t parity)
-{
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(parity));
-    return done;
-}
-
-// Bounded wait on an mbarrier phase: 1 when it completed, 0 when the poll limit ran out.
-__device__ __forceinline__ uint32_t tc_wait(uint32_t bar, uint32_t parity)
-{
-    for (long long spins = 0; spins < TC_WAIT_LIMIT; ++spins)
-        if (tc_try_wait(bar, parity)) return 1u;
-    return 0u;
 }
 
 // Bulk copy of one operand block into a stage; completes bytes on the stage's mbarrier.

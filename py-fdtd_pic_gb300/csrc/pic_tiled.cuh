@@ -82,6 +82,9 @@ __device__ __forceinline__ void st_release(int32_t *p, int v)
 {
     asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+// Per-run deadline set by fdtdpic_set_run_deadline (0: the default); defined in capi.cu.
+long long tiled_deadline_override_ns();
+
 __device__ __forceinline__ long long globaltimer()
 {
     long long t;
@@ -89,9 +92,15 @@ __device__ __forceinline__ long long globaltimer()
     return t;
 }
 
-// Thread 0 only.  true when *flag >= target; false after an abort or the deadline.
+// Thread 0 only.  true when *flag >= target; false after an abort or the deadline.  A wait that
+// starts after the deadline gives up at once, so a run past its time limit stops at its next
+// wait whether or not that wait would have to spin.
 __device__ inline bool tile_wait(const int32_t *flag, int target, int32_t *abort, long long deadline)
 {
+    if (globaltimer() > deadline) {
+        atomicCAS(abort, 0, FDTDPIC_ERR_TIMEOUT);
+        return false;
+    }
     for (long long it = 0; it < (1LL << 34); ++it) {
         if (ld_acquire(flag) >= target) return true;
         if ((it & 255) == 255) {
@@ -215,7 +224,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 1) pic_tiled_kernel(TileArgs<T> 
         if (tid == 0) {
             s_nstay = 0;
             for (int d = 0; d < MIG_DIRS; ++d) s_nout[d] = 0;
-            s_count = a.count[cur * a.G + b];
+            s_count = min(a.count[cur * a.G + b], a.cap);  // a bin overflow is reported, not read past
         }
         __syncthreads();
         const int np = s_count;
@@ -525,12 +534,12 @@ __global__ void tile_bin_kernel(int n_part, int G, int n, int cap, const int32_t
 }
 
 static __global__ void tile_offsets_kernel2(const int32_t *count, const int32_t *final_seg, int G,
-                                            int32_t *offs)
+                                            int cap, int32_t *offs)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         const int32_t *cnt = count + (size_t)(*final_seg) * G;
         int s = 0;
-        for (int b = 0; b < G; ++b) { offs[b] = s; s += cnt[b]; }
+        for (int b = 0; b < G; ++b) { offs[b] = s; s += min(cnt[b], cap); }
         offs[G] = s;
     }
 }
@@ -550,7 +559,7 @@ __global__ void tile_unbin_kernel(int G, int cap, const int32_t *count, const in
     const int b = blockIdx.x;
     if (b >= G) return;
     const int sgi = *final_seg;
-    const int cnt = count[(size_t)sgi * G + b], o = offs[b];
+    const int cnt = min(count[(size_t)sgi * G + b], cap), o = offs[b];
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
         const size_t r = (size_t)b * cap + i;
         const int d = o + i;
@@ -671,8 +680,11 @@ int launch_pic_tiled(int tsize, const FdtdInstance &h, const BatchArgs<T> &fa, c
     a.status = status;
     a.abort = (int32_t *)(scratch + S.abort);
     a.final_seg = (int32_t *)(scratch + S.final_seg);
-    // deadline for the whole run: 20 s plus 1 ms per step, far above any healthy run
+    // deadline for the whole run: 20 s plus 1 ms per step, far above any healthy run (a test
+    // may set a shorter one, fdtdpic_set_run_deadline)
     a.timeout_ns = 20LL * 1000 * 1000 * 1000 + 1000000LL * (h.step_end - h.step_begin);
+    const long long test_ns = tiled_deadline_override_ns();
+    if (test_ns > 0) a.timeout_ns = test_ns;
 
     const int threads = 256;
     const int nz1 = h.nz + 1;
@@ -715,7 +727,7 @@ int launch_pic_tiled(int tsize, const FdtdInstance &h, const BatchArgs<T> &fa, c
     }
     if (bm.n_part > 0) {
         int32_t *offs = (int32_t *)(scratch + S.offs);
-        tile_offsets_kernel2<<<1, 1, 0, st>>>(a.count, a.final_seg, g.G, offs);
+        tile_offsets_kernel2<<<1, 1, 0, st>>>(a.count, a.final_seg, g.G, g.cap, offs);
         tile_unbin_kernel<T><<<g.G, 256, 0, st>>>(g.G, g.cap, a.count, a.final_seg, offs, sg, cell,
                                                    frac, ux, uz, id, bm.n_part, status);
     }

@@ -34,6 +34,7 @@ UNITS = {
     "setup.cu": ["-fmad=false"],  # set-up products and sums round one by one, as numpy's
     "variants.cu": ["-fmad=false"],  # the uncalled ADE variants, rounded as the reference's
     "stepops.cu": ["-fmad=false"],  # per-step module functions, rounded as the reference's
+    "selftest.cu": [],  # the bounded waits' self-test
 }
 
 
@@ -204,6 +205,10 @@ def _declare(L):
     L.fdtdpic_step_op_check.argtypes = [P, P, c_i64]
     L.fdtdpic_step_op.restype = c_int
     L.fdtdpic_step_op.argtypes = [P, P, c_i64, P]
+    L.fdtdpic_set_run_deadline.restype = c_int
+    L.fdtdpic_set_run_deadline.argtypes = [c_i64]
+    L.fdtdpic_wait_selftest.restype = c_int
+    L.fdtdpic_wait_selftest.argtypes = [c_int, c_i64, P, P, P]
     for name, argt in _EXTRA_DECLS.items():
         if hasattr(L, name):
             fn = getattr(L, name)

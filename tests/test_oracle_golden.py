@@ -13,7 +13,8 @@ from oracle import oracle as O
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 CASES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-               if os.path.basename(p) not in ("cubic_solve.npz", "setup.npz", "variants.npz"))
+               if os.path.basename(p) not in ("cubic_solve.npz", "setup.npz", "variants.npz",
+                                              "stepops.npz"))
 
 # FP64 end-state fields and probe traces: the reference itself, to rounding.
 FIELD_TOL = 1e-12
