@@ -26,15 +26,19 @@
 
 namespace fdtdpic {
 
-// The update coefficients in the state type.  The curl coefficients (ue, uh, their slab values
-// and dt/dz) also keep the part of their FP64 value that T drops (*_lo: 0 in FP64): in FP32 a
-// coefficient rounded once is the same error at every cell and every step, a wave speed off by
-// up to 2^-24 whose phase error grows with the distance a pulse travels (a few 1e-5 relative
-// after the thousands of steps of the benchmarked runs); mul_c multiplies by the pair.
+// The update coefficients in the state type.  In FP32 a coefficient rounded once is the same
+// error at every cell and every step: a curl coefficient off by up to 2^-24 is a wave speed off
+// by as much, whose phase error grows with the distance a pulse travels (2e-5 relative on a
+// pulse after 8192 steps, 90% of it a shift of the whole pulse); the Lorentz recursion's A and
+// B sit within 1e-4 of 2 and -1, so their rounding moves the resonance.  The FP32 forms
+// therefore keep what FP32 drops: *_lo, the rest of the curl coefficients' FP64 values (mul_c
+// multiplies by the pair); e0r_rel / eps0_rel, the divisors' relative rounding; pa_m2 = A - 2
+// and pb_p1 = B + 1 in FP32 (pol_next).  In FP64 they are unused and every update keeps the
+// reference's operation order.
 template <typename T>
 struct Scal {
     T ue, ue_slab, uh, uh_slab, dtdz, eps0, pa, pb, pc, e0r, e0chi;
-    T ue_lo, ue_slab_lo, uh_lo, uh_slab_lo, dtdz_lo;
+    T ue_lo, ue_slab_lo, uh_lo, uh_slab_lo, dtdz_lo, e0r_rel, eps0_rel, pa_m2, pb_p1;
 };
 
 template <typename T>
@@ -49,13 +53,46 @@ __device__ inline Scal<T> make_scal(const FdtdInstance &I)
     s.uh_lo = (T)(I.uh - (double)s.uh);
     s.uh_slab_lo = (T)(I.uh_slab - (double)s.uh_slab);
     s.dtdz_lo = (T)(I.dtdz - (double)s.dtdz);
+    s.e0r_rel = (T)((I.nl_e0 - (double)s.e0r) / (double)s.e0r);
+    s.eps0_rel = (T)((I.eps0 - (double)s.eps0) / (double)s.eps0);
+    s.pa_m2 = (T)(I.pol_a - 2.0);
+    s.pb_p1 = (T)(I.pol_b + 1.0);
     return s;
 }
 
-// x times a curl coefficient (hi, lo): FP64 x * hi, the reference's product; FP32 the product
-// with the coefficient's FP64 value to ~48 bits, rounded once more than x * hi (unbiased).
+// x times a curl coefficient (hi, lo).  FP64: x * hi, the reference's product.  FP32: the fused
+// x * hi + (x * lo), one rounding of the product with the coefficient's ~48-bit value.  (The
+// other grouping, fl(x * hi) + x * lo, rounds back to fl(x * hi): the correction is below half
+// a unit in its last place.)
 __device__ __forceinline__ double mul_c(double x, double hi, double) { return x * hi; }
-__device__ __forceinline__ float mul_c(float x, float hi, float lo) { return fmaf(x, lo, x * hi); }
+__device__ __forceinline__ float mul_c(float x, float hi, float lo) { return fmaf(x, hi, x * lo); }
+
+// num / den where den is a constant of the instance plus a per-cell term: FP64 the plain
+// quotient; FP32 the quotient corrected by the constant's relative rounding rel (exact to first
+// order in rel, where rel <= 2^-24).
+__device__ __forceinline__ double div_c(double num, double den, double) { return num / den; }
+__device__ __forceinline__ float div_c(float num, float den, float rel)
+{
+    const float q = num / den;
+    return fmaf(-q, rel, q);
+}
+
+// The Lorentz recursion P_(n+1) = A P_n + B P_(n-1) + C E_n.  FP64 in the reference's order;
+// FP32 as (P_n + (P_n - P_(n-1))) + ((A - 2) P_n + (B + 1) P_(n-1) + C E_n), where A - 2 and
+// B + 1 are small and carry their own FP32 precision.
+template <typename T>
+__device__ __forceinline__ T pol_next(const Scal<T> &c, T p, T pm2, T ex);
+template <>
+__device__ __forceinline__ double pol_next(const Scal<double> &c, double p, double pm2, double ex)
+{
+    return c.pa * p + c.pb * pm2 + c.pc * ex;
+}
+template <>
+__device__ __forceinline__ float pol_next(const Scal<float> &c, float p, float pm2, float ex)
+{
+    const float small = fmaf(c.pa_m2, p, fmaf(c.pb_p1, pm2, c.pc * ex));
+    return (p + (p - pm2)) + small;
+}
 
 // PML table column of cell k, or -1.
 __device__ __forceinline__ int pml_col(const FdtdInstance &I, int k)
@@ -284,7 +321,7 @@ __device__ __forceinline__ void e_cell(const FdtdInstance &I, const Scal<T> &c, 
         const T pm2 = s.Pp(k);
         const T pcur = s.P(k);
         s.Pp(k) = pcur;
-        s.P(k) = c.pa * pcur + c.pb * pm2 + c.pc * ex;
+        s.P(k) = pol_next<T>(c, pcur, pm2, ex);
     }
     const int col = pml_col(I, k);
     const T den = (col >= 0) ? s.tab_at(FDTD_TAB_DENE, col) : T(1);
@@ -313,9 +350,9 @@ __device__ __forceinline__ void e_cell(const FdtdInstance &I, const Scal<T> &c, 
         if (I.mode == FDTD_MODE_KERR) {
             const T A = kr.root(dx, c.eps0, nfb);
             if (a_out) a_out[k] = A;
-            ex = dx / (c.e0r + c.e0chi * A);
+            ex = div_c(dx, c.e0r + c.e0chi * A, c.e0r_rel);
         } else {
-            ex = (dx - s.P(k)) / (c.eps0);
+            ex = div_c(dx - s.P(k), c.eps0, c.eps0_rel);
         }
     }
     s.Ex(k) = ex;

@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(256, 4) pic_e_kernel(PicField<T> a, int t_arg)
                 const T A = kr.root(d, c.eps0, &nfb);
                 if (a.last) gA[k] = A;
                 s.dx[k] = d;
-                s.ex[k] = d / (c.e0r + c.e0chi * A);
+                s.ex[k] = div_c(d, c.e0r + c.e0chi * A, c.e0r_rel);
             } else if (k >= 1) {
                 // PML, source and Lorentz cells: the whole e_cell on a register copy (their
                 // polarisation and psi loaded here)

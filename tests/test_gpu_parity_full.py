@@ -199,8 +199,13 @@ def test_sweep_sample_fp32_all_8192_steps():
     for j, (i, r) in enumerate(zip(pick, refs)):
         assert res[j].status == 0
         worst["fields"] = max(worst["fields"], O.rel_l2(res[j].Ex, r.Ex), O.rel_l2(res[j].Hy, r.Hy))
+        # both traces on the scale of the larger one: on the longest grids the pulse never
+        # reaches the far probe within 8192 steps, which then holds only a precursor ~1e-90
+        # (zero in FP32)
+        scale = max(np.linalg.norm(r.probes[:, 0]), np.linalg.norm(r.probes[:, 1]))
         for k in (0, 1):
-            worst["traces"] = max(worst["traces"], O.rel_l2(res[j].probes[:, k], r.probes[:, k]))
+            worst["traces"] = max(worst["traces"], float(
+                np.linalg.norm(res[j].probes[:, k] - r.probes[:, k]) / scale))
         want = r.probes.T @ W.T
         band = np.abs(want[0]) >= 1e-2 * np.abs(want[0]).max()
         want_r = np.abs(want[1]) / np.abs(want[0])
