@@ -154,3 +154,32 @@ def test_tiled_kernel_equals_streaming_kernels_bitwise(precision):
     np.testing.assert_array_equal(r1.probes(), r2.probes())
     for x, y in zip(a[-1][1], b[-1][1]):
         np.testing.assert_array_equal(x, y)
+
+
+@pytest.mark.parametrize("nz,clo,chi", [(512, 40, 480), (1536, 40, 1480)])
+def test_quad_push_equals_scalar_push_bitwise(nz, clo, chi):
+    """FP32 pushes over particle quads (chunks that are multiples of 4, aligned arrays) and the
+    one-particle-a-thread push (a chunk that is not) give the same bits: fields, currents (Jz
+    deposited on the last step), probes and particles; on the 1536-cell grid the push launches
+    carry the previous step's H phase."""
+    torch = _torch()
+    import scipy.constants as sc
+    from fdtdpic.grid import lorentz_kerr_grid
+    from fdtdpic.pic import PicRun, make_beam
+    out = []
+    for chunk in (0, 1022):
+        g = lorentz_kerr_grid(nz, T, front=300, rear=400, nzsrc=60, probes=(50, 350), chi3=1e-2)
+        beam = make_beam(NPART + 3, clo, chi, DZ)  # a ragged last quad
+        run = PicRun(g, beam, DZ, DT, sc.mu_0, precision="f32", chunk=chunk, path="streaming")
+        run.step(T)
+        torch.cuda.synchronize()
+        assert run.status()[0] == 0
+        out.append((run.fields(), run.currents(), run.probes(), run.particles()))
+    (fa, ja, pa, qa), (fb, jb, pb, qb) = out
+    for k in ("Ex", "Hy", "Dx", "A"):
+        np.testing.assert_array_equal(fa[k], fb[k], err_msg=k)
+    np.testing.assert_array_equal(ja[0], jb[0])
+    np.testing.assert_array_equal(ja[1], jb[1])
+    np.testing.assert_array_equal(pa, pb)
+    for x, y in zip(qa, qb):
+        np.testing.assert_array_equal(x, y)
