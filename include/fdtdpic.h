@@ -55,6 +55,8 @@ typedef struct CUstream_st *fdtdpic_stream_t; /* == cudaStream_t */
 #define FDTD_STATUS_SKIPPED 2   /* instance larger than smem_bytes: not run */
 #define FDTD_STATUS_TIMEOUT 4   /* beam step, tiled path: a bounded wait gave up */
 #define FDTD_STATUS_OVERFLOW 8  /* beam step, tiled path: a tile or migrant buffer overflowed */
+#define FDTD_STATUS_BOUNDS 16   /* the index-checking debug build (libfdtdpic_bounds.so) found an
+                                   index outside its buffer and skipped the access */
 
 /* PML coefficient table: per instance FDTD_TAB_ROWS rows x (2*pml+1) columns of doubles.
  * Column c <= pml is cell c; column c > pml is cell nz+1-pml+(c-pml-1). */

@@ -16,6 +16,7 @@
 
 #include <type_traits>
 
+#include "bounds.cuh"
 #include "fdtd1d_kernel.cuh"
 
 namespace fdtdpic {
@@ -294,11 +295,11 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long *arr, int idx, u
 template <int W>
 __device__ __forceinline__ void deposit_slot(unsigned long long *win, unsigned long long *acc,
                                              int nz1, int base, int word0, int node,
-                                             const long long *val)
+                                             const long long *val, int32_t *bounds = nullptr)
 {
     const int rel = node - base;
     const bool in_win = node >= 0 && rel >= 0 && rel < PIC_WIN;
-    const bool out = node >= 0 && !in_win;
+    const bool out = node >= 0 && !in_win && FDTD_IN(node, nz1, bounds);
 #pragma unroll
     for (int w = 0; w < W; ++w) {
         warp_add_u64(win + (size_t)(word0 + w) * PIC_WIN, in_win ? rel : -1,
@@ -620,8 +621,8 @@ __device__ __forceinline__ void push_deposit_jx(unsigned long long *win, const P
                 }
             }
         } else {
-            deposit_slot<W>(win, a.acc, nz1, base, 0, nx0, vx0);
-            deposit_slot<W>(win, a.acc, nz1, base, 0, nx1, vx1);
+            deposit_slot<W>(win, a.acc, nz1, base, 0, nx0, vx0, a.status + 1);
+            deposit_slot<W>(win, a.acc, nz1, base, 0, nx1, vx1, a.status + 1);
         }
     }
 }
@@ -705,6 +706,10 @@ __global__ void __launch_bounds__(PIC_THREADS, (FUSE_H && sizeof(T) == 4) ? 6 : 
         const int pn = p + blockDim.x;
         if (pn < b1) { nc = a.cell[pn]; nf = a.frac[pn]; nux = a.ux[pn]; nuz = a.uz[pn]; }
         if (valid && (c < 1 || c + 2 > a.nz)) { valid = false; ++lost; }
+        // debug build: the gathers' cells c-1 .. c+2 and the particle's slot
+        if (valid && !(FDTD_IN(c - 1, nz1, a.status + 1) && FDTD_IN(c + 2, nz1, a.status + 1) &&
+                       FDTD_IN(p, a.n_part, a.status + 1)))
+            valid = false;
         int nx0 = -1, nzA = -1, nzB = -1;
         T jx0 = T(0), jx1 = T(0);
         long long vzA[W], vzB[W];
@@ -760,8 +765,8 @@ __global__ void __launch_bounds__(PIC_THREADS, (FUSE_H && sizeof(T) == 4) ? 6 : 
         }
         push_deposit_jx<T>(win, a, nz1, base, lane, nx0, jx0, jx1);
         if (a.deposit_jz) {
-            deposit_slot<W>(win, a.acc, nz1, base, W, nzA, vzA);
-            deposit_slot<W>(win, a.acc, nz1, base, W, nzB, vzB);
+            deposit_slot<W>(win, a.acc, nz1, base, W, nzA, vzA, a.status + 1);
+            deposit_slot<W>(win, a.acc, nz1, base, W, nzB, vzB, a.status + 1);
         }
     }
     if (lost) atomicAdd(a.status, lost);
@@ -838,7 +843,8 @@ __global__ void __launch_bounds__(PIC_THREADS, 4)
     for (int r = 0; r < rounds; ++r) {
         const int qi = r * blockDim.x + threadIdx.x;
         const int p0 = b0 + PIC_QUAD * qi;
-        const int nv = max(0, min(PIC_QUAD, b1 - p0));  // valid particles of this quad
+        int nv = max(0, min(PIC_QUAD, b1 - p0));  // valid particles of this quad
+        if (nv > 0 && !FDTD_IN(p0 + nv - 1, a.n_part, a.status + 1)) nv = 0;
         int c4[PIC_QUAD];
         T f4[PIC_QUAD], x4[PIC_QUAD], z4[PIC_QUAD];
         if (nv == PIC_QUAD) {
@@ -877,6 +883,8 @@ __global__ void __launch_bounds__(PIC_THREADS, 4)
             const int c = c4[u];
             bool valid = u < nv;
             if (valid && (c < 1 || c + 2 > a.nz)) { valid = false; ++lost; }
+            if (valid && !(FDTD_IN(c - 1, nz1, a.status + 1) && FDTD_IN(c + 2, nz1, a.status + 1)))
+                valid = false;
             if (!valid) continue;
             if (c != wc) {
                 wc = c;
@@ -982,8 +990,8 @@ __global__ void __launch_bounds__(PIC_THREADS, 4)
         if constexpr (JZ) {
 #pragma unroll
             for (int u = 0; u < PIC_QUAD; ++u) {
-                deposit_slot<1>(win, a.acc, nz1, base, 1, nzA[u], &vzA[u]);
-                deposit_slot<1>(win, a.acc, nz1, base, 1, nzB[u], &vzB[u]);
+                deposit_slot<1>(win, a.acc, nz1, base, 1, nzA[u], &vzA[u], a.status + 1);
+                deposit_slot<1>(win, a.acc, nz1, base, 1, nzB[u], &vzB[u], a.status + 1);
             }
         }
     }
@@ -1169,6 +1177,7 @@ __global__ void pic_scatter_kernel(int n_part, const int32_t *cell, const T *fra
         const int h = run_head(heads, lane);
         const int q = __shfl_sync(0xffffffffu, base, h) + (lane - h);
         if (c < 0 || q >= n_part) continue;
+        if (!FDTD_IN(q, n_part, nullptr)) continue;
         cell2[q] = c;
         frac2[q] = f;
         ux2[q] = x;

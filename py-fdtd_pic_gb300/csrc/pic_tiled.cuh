@@ -272,6 +272,13 @@ __global__ void __launch_bounds__(TILE_THREADS, 1) pic_tiled_kernel(TileArgs<T> 
             const int c = cU[u];
             const T f = fU[u];
             if (valid && (c < c0 || c >= c1)) { atomicAdd(&s_lost, 1); valid = false; }
+            // debug build: the tile's shared arrays around c (gathers c-1 .. c+2, deposits
+            // c-1 .. c+2) and the particle's segment slot
+            if (valid && !(FDTD_IN(c - 1 - base, L, a.status + 1) &&
+                           FDTD_IN(c + 2 - base, L, a.status + 1) &&
+                           FDTD_IN(seg + (size_t)((it * U + u) * nt + tid), (size_t)a.G * a.cap,
+                                   a.status + 1)))
+                valid = false;
             int dir = -2;  // -2: nothing to write, -1: stays, 0..2: outbox
             int cn = 0, pid = 0;
             Moved<T> m;

@@ -16,8 +16,15 @@ PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(ROOT, "csrc")
 INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
-BUILD_DIR = os.path.join(ROOT, "_build")
-LIB_PATH = os.path.join(PKG_DIR, "libfdtdpic.so")
+# FDTDPIC_LIBRARY_VARIANT=bounds selects the index-checking debug build (libfdtdpic_bounds.so,
+# compiled with FDTDPIC_BOUNDS_CHECK: data-dependent indices are checked before use and a failed
+# check raises FDTD_STATUS_BOUNDS instead of touching memory); unset: the release build
+VARIANT = os.environ.get("FDTDPIC_LIBRARY_VARIANT", "")
+if VARIANT not in ("", "bounds"):
+    raise RuntimeError(f"FDTDPIC_LIBRARY_VARIANT={VARIANT!r}: expected 'bounds' or unset")
+_SUFFIX = "_bounds" if VARIANT == "bounds" else ""
+BUILD_DIR = os.path.join(ROOT, "_build" + _SUFFIX)
+LIB_PATH = os.path.join(PKG_DIR, f"libfdtdpic{_SUFFIX}.so")
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 # translation unit -> extra nvcc flags
@@ -66,6 +73,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     nvcc = _nvcc()
     common = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "-I", INCLUDE, "-I", CSRC]
+    if VARIANT == "bounds":
+        common.append("-DFDTDPIC_BOUNDS_CHECK")
 
     def compile_one(unit):
         obj = os.path.join(BUILD_DIR, unit.replace(".cu", ".o"))

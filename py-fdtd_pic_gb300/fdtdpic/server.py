@@ -115,12 +115,16 @@ class _Rejected(ValueError):
 
 @dataclass
 class _Big:
-    """A beam request running on the streaming kernels (side stream)."""
+    """A beam request running on the streaming kernels (side stream), a segment of steps at a
+    time; `snap` holds it on the host while it is parked."""
     req: Request
     run: object
     done_ev: object
     nbytes: int
     admitted: float
+    stream: object = None
+    snap: object = None
+    preempt: bool = False
 
 
 @dataclass
@@ -158,7 +162,7 @@ class Server:
     def __init__(self, precision="f32", hbm_budget=150e9, max_active=None, chunk_ms=3.0,
                  threads=512, smem_bytes=64 * 1024, max_inflight=2, keep_state=False,
                  max_admit_per_poll=64, prefetch=128, device=None, clock=time.perf_counter,
-                 big_ms=100.0, max_big=8, max_big_busy=2, fault_hook=None):
+                 big_ms=100.0, max_big=8, max_big_busy=2, fault_hook=None, big_segment=4096):
         _require_cuda()
         self.L = lib()
         check_slot_layout(self.L)
@@ -187,6 +191,14 @@ class Server:
         self.fault_hook = fault_hook
         self.cancelled: set = set()
         self.oom_retries = 0
+        # streaming runs advance big_segment steps per enqueue; at each segment's end a run is
+        # parked on the host (PicRun.snapshot, its device memory released) when more runs hold
+        # the GPU than the current streaming limit allows, or when preempt() asked for it, and
+        # resumed (PicRun.restore) ahead of new streaming admissions -- bit for bit the run it
+        # would have been
+        self.big_segment = max(1, int(big_segment))
+        self.parked: collections.deque = collections.deque()
+        self.preemptions = 0
         # rounds on a high-priority stream; each streaming-kernel request on a low-priority
         # stream of its own (its set-up's copies then wait for nothing else)
         self.stream = torch.cuda.Stream(device=self.dev, priority=-1)
@@ -354,6 +366,7 @@ class Server:
         """Admit prepared requests in arrival order while budget allows: streaming-kernel
         requests while fewer than max_big run, the others while slots are free."""
         admitted = 0
+        self._resume_parked(now)
         big_limit = streaming_limit(bool(self._ready), bool(self.free), self.max_big,
                                     self.max_big_busy)
         while len(self.big) < big_limit:
@@ -417,9 +430,10 @@ class Server:
             self._fail(req, now, f"out of device memory: {e}")
             return True
 
-    def _place_big(self, req: Request, need: int, now: float):
-        """Run a beam request on the streaming kernels, all its steps enqueued at once on a
-        low-priority stream of its own (graph blocks of 64 steps)."""
+    def _place_big(self, req: Request, need: int, now: float, parked: _Big = None):
+        """Run a beam request on the streaming kernels, on a low-priority stream of its own, a
+        segment of steps per enqueue (graph blocks of 64 steps); a parked run is restored from
+        its snapshot first."""
         g = req.grid
         req._host = None
         st = torch.cuda.Stream(device=self.dev, priority=0)
@@ -427,23 +441,80 @@ class Server:
             run = PicRun(g, req.beam, req.dz, req.dt, req.mu0,
                          precision="f64" if self.prec == F64 else "f32", path="streaming",
                          device=self.dev)
-            run.step(g.n_steps, stream=st)
+            if parked is not None:
+                run.restore(parked.snap)
+            run.step(self.big_segment, stream=st)
             ev = torch.cuda.Event()
             ev.record(st)
         self.bytes_in_use += need
-        self.big.append(_Big(req=req, run=run, done_ev=ev, nbytes=need, admitted=now))
+        if parked is None:
+            self.big.append(_Big(req=req, run=run, done_ev=ev, nbytes=need, admitted=now,
+                                 stream=st))
+        else:
+            parked.run, parked.done_ev, parked.stream, parked.snap = run, ev, st, None
+            parked.nbytes, parked.preempt = need, False
+            self.big.append(parked)
+
+    def preempt(self, rid: int) -> bool:
+        """Park streaming run ``rid`` at the end of its current segment (snapshot to the host,
+        device memory released); it resumes when the streaming limit allows.  False when no
+        such run is active."""
+        for b in self.big:
+            if b.req.rid == rid:
+                b.preempt = True
+                return True
+        return False
+
+    def _park(self, b: _Big):
+        b.snap = b.run.snapshot()  # synchronises the device; the segment has run
+        b.run = None
+        b.done_ev = None
+        self.bytes_in_use -= b.nbytes
+        self.big.remove(b)
+        self.parked.append(b)
+        self.preemptions += 1
+
+    def _resume_parked(self, now):
+        """Parked runs come back, oldest first, while the streaming limit and budget allow."""
+        limit = streaming_limit(bool(self._ready), bool(self.free), self.max_big,
+                                self.max_big_busy)
+        while self.parked and len(self.big) < limit:
+            b = self.parked[0]
+            need = self.big_request_bytes(b.req)
+            if not fits_budget(self.bytes_in_use, need, self.budget, bool(self.active or self.big)):
+                break
+            self.parked.popleft()
+            try:
+                self._place_big(b.req, need, now, parked=b)
+            except (torch.cuda.OutOfMemoryError, MemoryError):
+                self.parked.appendleft(b)
+                break
 
     def _complete_big(self, block=False):
         """Retire streaming-kernel requests whose work has run (the oldest first when
         blocking)."""
         n = 0
+        limit = streaming_limit(bool(self._ready), bool(self.free), self.max_big,
+                                self.max_big_busy)
         for b in list(self.big):
             if not b.done_ev.query():
                 if not block or n:
                     continue
                 b.done_ev.synchronize()
-            self.big.remove(b)
             run, g = b.run, b.req.grid
+            if run.step_done < g.n_steps and b.req.rid not in self.cancelled:
+                # a segment ended: park it (asked for, or more runs than the limit allows: the
+                # youngest go first), or enqueue its next segment
+                over = len(self.big) > limit and b is self.big[-1]
+                if b.preempt or over:
+                    self._park(b)
+                    continue
+                with torch.cuda.stream(b.stream):
+                    run.step(self.big_segment, stream=b.stream)
+                    b.done_ev = torch.cuda.Event()
+                    b.done_ev.record(b.stream)
+                continue
+            self.big.remove(b)
             st = run.status()
             status = np.zeros(4, np.int32)
             status[:2] = st[:2]
@@ -656,7 +727,7 @@ class Server:
 
     def drain(self):
         """Run until every submitted request has completed."""
-        while self.pending or self.active or self.inflight or self.big:
+        while self.pending or self.active or self.inflight or self.big or self.parked:
             self.poll()
             if not self.active and not self.pending:
                 if self.inflight:
@@ -685,7 +756,8 @@ class Server:
                 i += 1
             if now >= duration:
                 break
-            if not self.active and not self.pending and not self.inflight and not self.big:
+            if (not self.active and not self.pending and not self.inflight and not self.big
+                    and not self.parked):
                 if i >= len(reqs):
                     break
                 time.sleep(min(1e-3, max(0.0, reqs[i].arrival - now)))

@@ -133,3 +133,37 @@ def test_streaming_run_cancelled_is_discarded():
     assert done[0].error is None
     np.testing.assert_array_equal(done[0].probes, want.probes)
     assert srv.bytes_in_use == 0
+
+
+def test_preempted_streaming_runs_resume_bit_for_bit():
+    """Streaming runs advance a segment at a time; two of three are parked on the host at a
+    segment's end (PicRun.snapshot, device memory released) and resumed later (restore): every
+    result equals the same request run without interruption, bit for bit."""
+    _torch()
+    from fdtdpic.server import Server
+
+    def serve(preempt):
+        srv = Server(precision="f32", keep_state=True, big_ms=0.0, big_segment=64)
+        srv.submit(_req(1, 2500, 1500, 3000))  # 24 segments of 64 steps
+        srv.submit(_req(3, *SPECS[3]))
+        srv.submit(_req(9, 700, 2000, 20000))   # 32 segments
+        srv.poll()
+        while len(srv.big) < 3 and srv.pending:  # the preparation thread hands them over
+            srv.poll()
+        if preempt:
+            assert srv.preempt(1) and srv.preempt(9)
+        done = {d.rid: d for d in srv.drain()}
+        srv.close()
+        return srv, done
+
+    srv0, want = serve(False)
+    srv1, got = serve(True)
+    assert srv0.preemptions == 0 and srv1.preemptions >= 2
+    for i in (1, 3, 9):
+        assert got[i].error is None
+        np.testing.assert_array_equal(got[i].probes, want[i].probes)
+        np.testing.assert_array_equal(got[i].fields["Ex"], want[i].fields["Ex"])
+        np.testing.assert_array_equal(got[i].fields["Jx"], want[i].fields["Jx"])
+        for k in ("cell", "frac", "ux", "uz"):
+            np.testing.assert_array_equal(got[i].particles[k], want[i].particles[k])
+    assert srv1.bytes_in_use == 0 and not srv1.parked
