@@ -183,8 +183,8 @@ int fdtdpic_dft_probes(int precision, const void *d_traces, int R, int S, int rp
                        int64_t sp, int64_t sn, const void *d_tw, int F, double *d_out,
                        fdtdpic_stream_t stream);
 /* The same X on the tensor cores (tcgen05, sm_103a): split-BF16x3 products (about 16
- * significant bits each) with FP32 sums over 256-step groups in tensor memory and FP64 sums
- * across groups.  The operands are first packed into BF16 tiles in d_scratch (16-byte aligned,
+ * significant bits each) with FP32 sums over 1024-step groups in tensor memory and compensated
+ * FP32 sums (an error-free two-sum into a float pair, ~48 bits) across groups.  The operands are first packed into BF16 tiles in d_scratch (16-byte aligned,
  * fdtdpic_dft_tc_scratch_bytes(R, S, F) bytes).  d_err (one int32, caller-zeroed) is set
  * non-zero if a bounded wait for the copies or the tensor cores gave up (the affected outputs
  * are then not written). */

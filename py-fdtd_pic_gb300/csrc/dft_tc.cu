@@ -7,7 +7,9 @@
 // fdtdpic_dft_probes).  Each operand is split into two BF16 halves, x = xh + xl and
 // B = Bh + Bl (xl = bf16(x - xh)), and C ~= xh Bh + xh Bl + xl Bh: three BF16 MMAs per K step,
 // about 16 significant bits per product, FP32 sums in tensor memory over TC_FLUSH chunks of
-// TC_KC steps, then FP64 sums in shared memory (FP32 rounding is bounded by one flush group).
+// TC_KC steps, then compensated FP32 sums (a float pair per output, error-free two-sum) in
+// shared memory: the group sums' rounding is bounded by one flush group of 1024 steps, and the
+// sums across groups keep ~48 bits without the narrow FP64 pipe.
 //
 // Three launches:
 //   dft_tc_pack_traces   traces -> BF16 hi/lo operand tiles, one 32 KiB block per (128 traces,
@@ -34,7 +36,7 @@ constexpr int TC_N = 64;           // output columns per CTA (32 frequencies x r
 constexpr int TC_Q = TC_N / 2;     // frequencies per CTA
 constexpr int TC_KC = 64;          // time steps per chunk (one pipeline stage)
 constexpr int TC_KSTEP = 16;       // K of one kind::f16 MMA
-constexpr int TC_FLUSH = 4;        // chunks summed in FP32 before the FP64 sums
+constexpr int TC_FLUSH = 16;       // chunks summed in FP32 before the compensated sums
 constexpr int TC_THREADS = 128;
 constexpr int TC_TMEM_COLS = 64;   // FP32 accumulator columns (power of two >= 32)
 constexpr uint32_t TC_LBO = 128;                          // next core matrix along K
@@ -44,7 +46,7 @@ constexpr uint32_t TC_B_HALF = (TC_N / 8) * TC_SBO;        // 8 KiB
 constexpr uint32_t TC_A_BLOCK = 2 * TC_A_HALF;             // hi then lo
 constexpr uint32_t TC_B_BLOCK = 2 * TC_B_HALF;
 constexpr uint32_t TC_STAGE = TC_A_BLOCK + TC_B_BLOCK;     // 48 KiB
-constexpr uint32_t TC_ACC_BYTES = TC_M * TC_N * 8;         // FP64 tile, 64 KiB
+constexpr uint32_t TC_ACC_BYTES = TC_M * TC_N * 8;         // float-pair tile, 64 KiB
 constexpr uint32_t TC_SMEM = 2 * TC_STAGE + TC_ACC_BYTES + 64;
 
 // Byte offset of element (row, k) of a K-major operand tile in the core-matrix layout.
@@ -182,7 +184,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                   int F, double *out, int32_t *err)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
-    double *acc = reinterpret_cast<double *>(sm + 2 * TC_STAGE);  // [TC_N][TC_M]
+    float2 *acc = reinterpret_cast<float2 *>(sm + 2 * TC_STAGE);  // [TC_N][TC_M] (sum, error)
     uint64_t *bars = reinterpret_cast<uint64_t *>(acc + TC_M * TC_N);  // full[0], full[1], mma
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 3);
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -191,7 +193,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const unsigned char *a_src = a_tiles + (int64_t)rt * n_kc * TC_A_BLOCK;
     const unsigned char *b_src = b_tiles + (int64_t)ct * n_kc * TC_B_BLOCK;
 
-    for (int i = tid; i < TC_M * TC_N; i += TC_THREADS) acc[i] = 0.0;
+    for (int i = tid; i < TC_M * TC_N; i += TC_THREADS) acc[i] = make_float2(0.f, 0.f);
     const uint32_t s_base = (uint32_t)__cvta_generic_to_shared(sm);
     const uint32_t full0 = (uint32_t)__cvta_generic_to_shared(bars);
     const uint32_t mma_bar = full0 + 16;
@@ -257,7 +259,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
         if ((c % TC_FLUSH) == TC_FLUSH - 1 || c == n_kc - 1) {
-            // this thread's row of the FP32 accumulator -> FP64 sums
+            // this thread's row of the FP32 accumulator -> the compensated sums
 #pragma unroll
             for (int c0 = 0; c0 < TC_N; c0 += 16) {
                 uint32_t v[16];
@@ -270,8 +272,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     : "r"(t_row + (uint32_t)c0));
                 asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    acc[(c0 + j) * TC_M + tid] += (double)__uint_as_float(v[j]);
+                for (int j = 0; j < 16; ++j) {
+                    float2 &a2 = acc[(c0 + j) * TC_M + tid];
+                    const float b = __uint_as_float(v[j]);
+                    const float s2 = __fadd_rn(a2.x, b);  // two-sum: s2 + e == a2.x + b exactly
+                    const float bp = __fsub_rn(s2, a2.x);
+                    const float e = __fadd_rn(__fsub_rn(a2.x, __fsub_rn(s2, bp)), __fsub_rn(b, bp));
+                    a2.x = s2;
+                    a2.y = __fadd_rn(a2.y, e);
+                }
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
@@ -299,7 +308,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (r < R)
         for (int c = 0; c < TC_N; ++c) {
             const int f = q0 + (c >> 1);
-            if (f < F) out[((int64_t)r * F + f) * 2 + (c & 1)] = acc[c * TC_M + tid];
+            if (f < F) {
+                const float2 a2 = acc[c * TC_M + tid];
+                out[((int64_t)r * F + f) * 2 + (c & 1)] = (double)a2.x + (double)a2.y;
+            }
         }
 }
 
