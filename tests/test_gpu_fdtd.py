@@ -105,15 +105,18 @@ def test_batch_equals_alone_and_is_deterministic():
 
 def test_fp32_error_vs_fp64_oracle():
     """FP32 state (FP64 only for near-degenerate cubics) against the reference's FP64 outputs
-    over 4096 steps: 1e-5 relative L2 on the final fields, 5e-5 on the probe traces."""
-    for name in ("kerr_nz1000", "lorentz_nz1000"):
+    over 4096 steps.  Kerr: 1e-5 relative L2 on the final fields.  Lorentz (two passes, the
+    second with the polarisation on): 2e-5, because its E = (Dx - P)/eps0 subtracts two values
+    about (1 + d_eps) = 3 and d_eps = 2 times E, so FP32 rounding of Dx and P reaches E three
+    times larger.  Probe traces 5e-5."""
+    for name, bound in (("kerr_nz1000", 1e-5), ("lorentz_nz1000", 2e-5)):
         g, grids, res = _run_golden(name, "f32")
         last = res[-1]
         want = g["Port2"] if name.startswith("kerr") else g["x1ColAf"]
         e = dict(Ex=O.rel_l2(last.Ex, g["Ex"]), Hy=O.rel_l2(last.Hy, g["Hy"]),
                  trace=O.rel_l2(last.probes[:, 1], want))
         print(f"\n{name} FP32 vs reference: " + ", ".join(f"{k} {v:.3e}" for k, v in e.items()))
-        assert e["Ex"] <= 1e-5 and e["Hy"] <= 1e-5, (name, e)
+        assert e["Ex"] <= bound and e["Hy"] <= bound, (name, e)
         assert e["trace"] <= 5e-5, (name, e)
 
 

@@ -161,15 +161,24 @@ def _sweep_sample(n_pick=32):
     return spec, params, pick
 
 
+HIST = 512  # snapshot interval of the sweep sample: 16 snapshots of Ex over the 8192 steps
+
+
 def test_sweep_sample_fp32_all_8192_steps():
     """32 grids of the 4096-grid sweep (its smallest, its largest and 30 between by Nz), FP32,
-    8192 steps, tensor-core DFT, against the FP64 oracle's fields, traces and |R(f)|."""
+    8192 steps, tensor-core DFT, against the FP64 oracle.  Fields: the relative L2 error of Ex
+    over the run (its snapshots every 512 steps, space and time together), and the final Ex and
+    Hy against the largest field norm of the run (on the shorter grids the pulse has left by
+    step 8192 and the final field is a residual a few percent of the pulse, whose own relative
+    error says little); probe traces, |R(f)|."""
     torch = _torch()
     import scipy.constants as sc
     from fdtdpic import engine, sweep
     spec, params, pick = _sweep_sample()
     grids_all, dt = sweep.make_sweep_grids(spec)
     grids = [grids_all[i] for i in pick]
+    for g in grids:
+        g.hist_interval, g.hist_rows = HIST, spec.n_steps // HIST
     sw = sweep.Sweep(grids, dt, spec.freqs(), precision="f32", dft="tc")
     sw.run()
     torch.cuda.synchronize()
@@ -189,16 +198,23 @@ def test_sweep_sample_fp32_all_8192_steps():
                         freq_in=spec.freq_in, permit_0=sc.epsilon_0, permea_0=sc.mu_0,
                         nonLinMed=True, FreeSpace=False, plasmaFreqE=np.sqrt(p["d_eps"]) * w0,
                         omega_0E=w0, gammaE=2 * np.pi * 0.1e9, chi3Stat=p["chi3"],
-                        sigmaOpt=O.sigma_opt(sweep.DZ, sc.epsilon_0, sc.mu_0))
+                        sigmaOpt=O.sigma_opt(sweep.DZ, sc.epsilon_0, sc.mu_0), vidInterval=HIST)
         return O.integrate(P, O.KERR, grids_all[i].exs, np.zeros(spec.n_steps),
                            extra_probes=p["probes"])
 
     with ThreadPoolExecutor(THREADS) as ex:  # the oracle's C loop releases the GIL
         refs = list(ex.map(oracle_one, pick))
-    worst = dict(fields=0.0, traces=0.0, refl=0.0)
+    worst = dict(history=0.0, final=0.0, final_rel=0.0, traces=0.0, refl=0.0)
     for j, (i, r) in enumerate(zip(pick, refs)):
         assert res[j].status == 0
-        worst["fields"] = max(worst["fields"], O.rel_l2(res[j].Ex, r.Ex), O.rel_l2(res[j].Hy, r.Hy))
+        h_gpu, h_ref = res[j].hist, r.Ex_History
+        assert h_gpu is not None and h_gpu.shape == h_ref.shape
+        worst["history"] = max(worst["history"], O.rel_l2(h_gpu, h_ref))
+        scale = max(np.linalg.norm(h_ref, axis=1).max(), np.linalg.norm(r.Ex))
+        hscale = scale * np.linalg.norm(r.Hy) / max(np.linalg.norm(r.Ex), 1e-300)
+        worst["final"] = max(worst["final"], float(np.linalg.norm(res[j].Ex - r.Ex) / scale),
+                             float(np.linalg.norm(res[j].Hy - r.Hy) / max(hscale, 1e-300)))
+        worst["final_rel"] = max(worst["final_rel"], O.rel_l2(res[j].Ex, r.Ex))
         # both traces on the scale of the larger one: on the longest grids the pulse never
         # reaches the far probe within 8192 steps, which then holds only a precursor ~1e-90
         # (zero in FP32)
@@ -214,7 +230,7 @@ def test_sweep_sample_fp32_all_8192_steps():
     nzs = [params[i]["nz"] for i in pick]
     print(f"\nsweep sample: {len(pick)} grids, Nz {min(nzs)}..{max(nzs)}")
     _report("sweep FP32, 8192 steps", worst,
-            dict(fields=F32_FIELDS, traces=F32_TRACES, refl=F32_REFL))
+            dict(history=F32_FIELDS, final=F32_FIELDS, traces=F32_TRACES, refl=F32_REFL))
 
 
 @pytest.fixture(scope="module")
