@@ -14,7 +14,6 @@
 #include <limits.h>
 #include <stdint.h>
 
-#include <type_traits>
 
 #include "bounds.cuh"
 #include "fdtd1d_kernel.cuh"
@@ -779,232 +778,6 @@ __global__ void __launch_bounds__(PIC_THREADS, (FUSE_H && sizeof(T) == 4) ? 6 : 
     }
 }
 
-// FP32 push over quads: each thread takes four consecutive particles, loaded and stored as one
-// 16-byte vector per array, and keeps the field values around its current cell in registers
-// (consecutive particles of a sorted beam nearly always share a cell).  When a lane's four
-// particles deposit on one node pair with words below 2^24 the lane sums them first, and a warp
-// whose lanes all hit the same pair sums the lane sums with one reduction per node; anything
-// else deposits particle slot by particle slot as pic_push_kernel does.  Each particle's
-// arithmetic is pic_push_kernel's (the same gathered values, particle_step, the same integer
-// deposit words), and integer sums do not depend on grouping, so the results are the same bits.
-// Needs 16-byte aligned particle arrays and a chunk that is a multiple of 4 (the host checks).
-// JZ: the call's last step, which also deposits Jz (a.deposit_jz set).
-constexpr int PIC_QUAD = 4;
-
-template <bool FUSE_H, bool JZ>
-__global__ void __launch_bounds__(PIC_THREADS, 4)
-    pic_push4_kernel(PicArgs<float> a, PicField<float> hf, int th)
-{
-    using T = float;
-    __shared__ unsigned long long win[2 * PIC_WIN];
-    __shared__ int base_s;
-    __shared__ HOnTheFly<T> q_s;
-    pdl_trigger();
-    int blk = blockIdx.x;
-    if constexpr (FUSE_H) {
-        if (blk < a.hblocks) {
-            pic_h_body<T, FIELD_UH_FUSED>(hf, th, blk, a.hblocks);
-            return;
-        }
-        blk -= a.hblocks;
-    }
-    const int b0 = blk * a.chunk;
-    const int b1 = min(a.n_part, b0 + a.chunk);
-    if (b0 >= b1) return;
-    const int nz1 = a.nz + 1;
-    const int win_words = (JZ ? 2 : 1) * PIC_WIN;
-    for (int i = threadIdx.x; i < win_words; i += blockDim.x) win[i] = 0ull;
-    if constexpr (FUSE_H) {
-        if (threadIdx.x == 0) {
-            const FdtdInstance &I = hf.f.inst[0];
-            HOnTheFly<T> q;
-            q.src_h = src_h_at<T>(I, hf.f.src, pic_step_index(hf, th));
-            q.uh = hf.fc->c.uh;
-            q.uh_slab = hf.fc->c.uh_slab;
-            q.uh_lo = hf.fc->c.uh_lo;
-            q.uh_slab_lo = hf.fc->c.uh_slab_lo;
-            q.tfsf_cell = I.tfsf ? I.nzsrc - 1 : INT_MIN;
-            const bool fs = I.mode == FDTD_MODE_FREESPACE;
-            q.slab_lo = fs ? I.front : 0;
-            q.slab_hi = fs ? I.rear : 0;
-            q.plain = !I.tfsf && !fs;
-            q_s = q;
-        }
-    }
-    pdl_wait();  // the previous step's fields and particles
-    if (threadIdx.x == 0) base_s = a.cell[b0] - 8;
-    __syncthreads();
-    const int base = base_s;
-    const int Lc = a.chi - a.clo;
-    const int lane = threadIdx.x & 31;
-    const int nq = (b1 - b0 + PIC_QUAD - 1) / PIC_QUAD;
-    const int rounds = (nq + blockDim.x - 1) / blockDim.x;  // warp-uniform
-    int lost = 0;
-    for (int r = 0; r < rounds; ++r) {
-        const int qi = r * blockDim.x + threadIdx.x;
-        const int p0 = b0 + PIC_QUAD * qi;
-        int nv = max(0, min(PIC_QUAD, b1 - p0));  // valid particles of this quad
-        if (nv > 0 && !FDTD_IN(p0 + nv - 1, a.n_part, a.status + 1)) nv = 0;
-        int c4[PIC_QUAD];
-        T f4[PIC_QUAD], x4[PIC_QUAD], z4[PIC_QUAD];
-        if (nv == PIC_QUAD) {
-            const int4 cv = *reinterpret_cast<const int4 *>(a.cell + p0);
-            const float4 fv = *reinterpret_cast<const float4 *>(a.frac + p0);
-            const float4 xv = *reinterpret_cast<const float4 *>(a.ux + p0);
-            const float4 zv = *reinterpret_cast<const float4 *>(a.uz + p0);
-            c4[0] = cv.x; c4[1] = cv.y; c4[2] = cv.z; c4[3] = cv.w;
-            f4[0] = fv.x; f4[1] = fv.y; f4[2] = fv.z; f4[3] = fv.w;
-            x4[0] = xv.x; x4[1] = xv.y; x4[2] = xv.z; x4[3] = xv.w;
-            z4[0] = zv.x; z4[1] = zv.y; z4[2] = zv.z; z4[3] = zv.w;
-        } else {
-#pragma unroll
-            for (int u = 0; u < PIC_QUAD; ++u) {
-                const bool in = u < nv;
-                c4[u] = in ? a.cell[p0 + u] : 0;
-                f4[u] = in ? a.frac[p0 + u] : T(0);
-                x4[u] = in ? a.ux[p0 + u] : T(0);
-                z4[u] = in ? a.uz[p0 + u] : T(0);
-            }
-        }
-        // the fields around the current cell wc: E at wc-1..wc+2 and, at the half nodes
-        // wc-1..wc+1, H one half step back and H^(t+1/2) (formed here from them and E when the
-        // launch carries the H phase, read from Hy otherwise)
-        int wc = INT_MIN;
-        T e[4], hp[3], hn[3];
-        int nx[PIC_QUAD];
-        T jx0[PIC_QUAD], jx1[PIC_QUAD];
-        int nzA[JZ ? PIC_QUAD : 1], nzB[JZ ? PIC_QUAD : 1];
-        long long vzA[JZ ? PIC_QUAD : 1], vzB[JZ ? PIC_QUAD : 1];
-#pragma unroll
-        for (int u = 0; u < PIC_QUAD; ++u) {
-            nx[u] = -1;
-            jx0[u] = jx1[u] = T(0);
-            if constexpr (JZ) { nzA[u] = nzB[u] = -1; vzA[u] = vzB[u] = 0; }
-            const int c = c4[u];
-            bool valid = u < nv;
-            if (valid && (c < 1 || c + 2 > a.nz)) { valid = false; ++lost; }
-            if (valid && !(FDTD_IN(c - 1, nz1, a.status + 1) && FDTD_IN(c + 2, nz1, a.status + 1)))
-                valid = false;
-            if (!valid) continue;
-            if (c != wc) {
-                wc = c;
-                if constexpr (FUSE_H) {
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) e[i] = __ldg(a.ex + c - 1 + i);
-                } else {
-                    e[1] = __ldg(a.ex + c);
-                    e[2] = __ldg(a.ex + c + 1);
-                }
-#pragma unroll
-                for (int i = 0; i < 3; ++i) hp[i] = __ldg(a.hyp + c - 1 + i);
-                if constexpr (FUSE_H) {
-                    const HOnTheFly<T> &q = q_s;
-#pragma unroll
-                    for (int i = 0; i < 3; ++i)
-                        hn[i] = q.plain ? hp[i] + mul_c(e[i + 1] - e[i], q.uh, q.uh_lo)
-                                        : h_on_the_fly<T>(q, c - 1 + i, hp[i], e[i], e[i + 1]);
-                } else {
-#pragma unroll
-                    for (int i = 0; i < 3; ++i) hn[i] = __ldg(a.hy + c - 1 + i);
-                }
-            }
-            const T f = f4[u];
-            const bool up = f >= T(0.5);  // j = c (nodes c, c+1) or c - 1 (nodes c-1, c)
-            const T fh = up ? f - T(0.5) : f + T(0.5);
-            const T E = (T(1) - f) * e[1] + f * e[2];
-            const T n0 = up ? hn[1] : hn[0], n1 = up ? hn[2] : hn[1];
-            const T p0v = up ? hp[1] : hp[0], p1v = up ? hp[2] : hp[1];
-            const T H = (T(1) - fh) * (T(0.5) * (n0 + p0v)) + fh * (T(0.5) * (n1 + p1v));
-            Moved<T> m;
-            particle_step<T>(E, H, c, f, x4[u], z4[u], a.kE, a.kH, a.sc, a.kJ, m);
-            nx[u] = m.nx0;
-            jx0[u] = m.jx0;
-            jx1[u] = m.jx1;
-            if constexpr (JZ) {
-                const MovedJz<T> z = particle_jz<T>(c, f, m, a.kJz);
-                nzA[u] = z.nzA;
-                nzB[u] = z.nzB;
-                long long w;
-                Fix<T>::split(z.jzA, a.jscale, a.jscale_f, &w);
-                vzA[u] = w;
-                if (z.nzB >= 0) {
-                    Fix<T>::split(z.jzB, a.jscale, a.jscale_f, &w);
-                    vzB[u] = w;
-                }
-            }
-            int c1 = m.c1;
-            if (c1 >= a.chi) c1 -= Lc;
-            else if (c1 < a.clo) c1 += Lc;
-            c4[u] = c1;
-            f4[u] = m.f1;
-            x4[u] = m.ux;
-            z4[u] = m.uz;
-        }
-        // stores (a particle that left the grid keeps its values, as in pic_push_kernel)
-        if (nv == PIC_QUAD) {
-            *reinterpret_cast<int4 *>(a.cell + p0) = make_int4(c4[0], c4[1], c4[2], c4[3]);
-            *reinterpret_cast<float4 *>(a.frac + p0) = make_float4(f4[0], f4[1], f4[2], f4[3]);
-            *reinterpret_cast<float4 *>(a.ux + p0) = make_float4(x4[0], x4[1], x4[2], x4[3]);
-            *reinterpret_cast<float4 *>(a.uz + p0) = make_float4(z4[0], z4[1], z4[2], z4[3]);
-        } else {
-#pragma unroll
-            for (int u = 0; u < PIC_QUAD; ++u) {
-                if (u < nv) {
-                    a.cell[p0 + u] = c4[u]; a.frac[p0 + u] = f4[u];
-                    a.ux[p0 + u] = x4[u]; a.uz[p0 + u] = z4[u];
-                }
-            }
-        }
-        // Jx deposits
-        bool any = false;
-#pragma unroll
-        for (int u = 0; u < PIC_QUAD; ++u) any = any || jx0[u] != T(0) || jx1[u] != T(0);
-        if (__any_sync(0xffffffffu, any)) {
-            // a lane whose four particles share one node pair with words below 2^24 sums them
-            bool one = nv == PIC_QUAD;
-            int s0 = 0, s1 = 0;
-#pragma unroll
-            for (int u = 0; u < PIC_QUAD; ++u) {
-                const float x0 = jx0[u] * a.jscale_f, x1 = jx1[u] * a.jscale_f;
-                one = one && nx[u] == nx[0] && nx[u] >= 0 && fabsf(x0) < 16777216.f &&
-                      fabsf(x1) < 16777216.f;
-                s0 += __float2int_rn(x0);  // used only when every term is below 2^24
-                s1 += __float2int_rn(x1);
-            }
-            const int i0 = __shfl_sync(0xffffffffu, nx[0], 0);
-            const int r0 = i0 - base;
-            if (__all_sync(0xffffffffu, one && nx[0] == i0) && r0 >= 0 && r0 + 1 < PIC_WIN) {
-                // 32 lanes of sums below 2^26: exact in 32 bits
-                const int w0 = __reduce_add_sync(0xffffffffu, s0);
-                const int w1 = __reduce_add_sync(0xffffffffu, s1);
-                if (lane == 0) {
-                    if (w0 != 0) smem_add_u64(win + r0, (unsigned long long)(long long)w0);
-                    if (w1 != 0) smem_add_u64(win + r0 + 1, (unsigned long long)(long long)w1);
-                }
-            } else {
-#pragma unroll
-                for (int u = 0; u < PIC_QUAD; ++u)
-                    push_deposit_jx<T>(win, a, nz1, base, lane, nx[u], jx0[u], jx1[u]);
-            }
-        }
-        if constexpr (JZ) {
-#pragma unroll
-            for (int u = 0; u < PIC_QUAD; ++u) {
-                deposit_slot<1>(win, a.acc, nz1, base, 1, nzA[u], &vzA[u], a.status + 1);
-                deposit_slot<1>(win, a.acc, nz1, base, 1, nzB[u], &vzB[u], a.status + 1);
-            }
-        }
-    }
-    if (lost) atomicAdd(a.status, lost);
-    __syncthreads();
-    for (int i = threadIdx.x; i < win_words; i += blockDim.x) {
-        const unsigned long long v = win[i];
-        const int word = i / PIC_WIN;
-        const int node = base + (i % PIC_WIN);
-        if (v != 0ull && node >= 0 && node < nz1) atomicAdd(a.acc + (size_t)word * nz1 + node, v);
-    }
-}
-
 // The device step counter: set before the first replayed block, advanced by a block's length
 // at the end of each block (one launch per block, not per step).
 static __global__ void pic_advance_kernel(int32_t *step, int k) { *step += k; }
@@ -1251,7 +1024,6 @@ struct PicPlan {
     int threads, fblocks, pblocks, sblocks, nz1;
     bool fused;
     bool fuse_h;  // the push launch carries the previous step's H phase (pic_push_kernel FUSE_H)
-    bool quad;    // FP32 push over particle quads (pic_push4_kernel)
     PicArgs<T> pa;
     PicField<T> pf;
     int32_t *counts, *cursor, *step, *tile_sum;
@@ -1318,26 +1090,10 @@ void pic_enqueue_step(PicPlan<T> &P, const PicBeam &bm, int t, bool do_sort, boo
         if (!with_h) pic_flush_h(P, ph, st, tm);
         P.pa.hblocks = with_h ? P.fblocks : 0;
         const int grid = P.pblocks + (with_h ? P.fblocks : 0);
-        const PicField<T> &hf = with_h ? ph.pf : P.pf;
-        const int th = with_h ? ph.t : 0;
-        bool launched = false;
-        if constexpr (std::is_same<T, float>::value) {
-            if (P.quad) {
-                if (with_h)
-                    launch_pdl(last_step ? pic_push4_kernel<true, true> : pic_push4_kernel<true, false>,
-                               grid, PIC_THREADS, st, P.pa, hf, th);
-                else
-                    launch_pdl(last_step ? pic_push4_kernel<false, true> : pic_push4_kernel<false, false>,
-                               grid, PIC_THREADS, st, P.pa, hf, th);
-                launched = true;
-            }
-        }
-        if (!launched) {
-            if (with_h)
-                launch_pdl(pic_push_kernel<T, true>, grid, PIC_THREADS, st, P.pa, hf, th);
-            else
-                launch_pdl(pic_push_kernel<T, false>, grid, PIC_THREADS, st, P.pa, hf, th);
-        }
+        if (with_h)
+            launch_pdl(pic_push_kernel<T, true>, grid, PIC_THREADS, st, P.pa, ph.pf, ph.t);
+        else
+            launch_pdl(pic_push_kernel<T, false>, grid, PIC_THREADS, st, P.pa, P.pf, 0);
         if (with_h) ph.on = false;
         if (tm) tm->end();
     } else {
@@ -1436,21 +1192,6 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
         // best on GB300 for a one-to-two-wave beam; 1024 for many waves)
         if (P.fuse_h && bm.chunk == 0) {
             pa.chunk = 768;
-            P.pblocks = (bm.n_part + pa.chunk - 1) / pa.chunk;
-        }
-    }
-    // FP32 push over particle quads when every particle array (the caller's and the scratch
-    // copies) is 16-byte aligned and the chunk is a multiple of 4: 1024 particles a CTA, one
-    // quad a thread
-    P.quad = false;
-    if constexpr (std::is_same<T, float>::value) {
-        const uintptr_t any = (uintptr_t)cell | (uintptr_t)frac | (uintptr_t)ux | (uintptr_t)uz |
-                              (uintptr_t)P.cellB | (uintptr_t)P.fracB | (uintptr_t)P.uxB |
-                              (uintptr_t)P.uzB;
-        const int qchunk = bm.chunk > 0 ? bm.chunk : 1024;
-        if (bm.n_part > 0 && any % 16 == 0 && qchunk % PIC_QUAD == 0) {
-            P.quad = true;
-            pa.chunk = qchunk;
             P.pblocks = (bm.n_part + pa.chunk - 1) / pa.chunk;
         }
     }

@@ -1,7 +1,7 @@
 """The index-checking debug build (libfdtdpic_bounds.so, FDTDPIC_BOUNDS_CHECK): every
 data-dependent index of the beam kernels is checked before use and a failed check raises
-FDTD_STATUS_BOUNDS instead of touching memory.  Beam runs on the streaming kernels (one particle
-a thread and particle quads, with the push launches carrying the H phase), on the persistent
+FDTD_STATUS_BOUNDS instead of touching memory.  Beam runs on the streaming kernels (with a
+ragged chunk, and with the push launches carrying the H phase), on the persistent
 tiled kernel, and in FP64, run in a child process on that build: no check fails, and every
 result equals the release build's bit for bit (the checks change no arithmetic)."""
 import os

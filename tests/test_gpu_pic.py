@@ -157,11 +157,11 @@ def test_tiled_kernel_equals_streaming_kernels_bitwise(precision):
 
 
 @pytest.mark.parametrize("nz,clo,chi", [(512, 40, 480), (1536, 40, 1480)])
-def test_quad_push_equals_scalar_push_bitwise(nz, clo, chi):
-    """FP32 pushes over particle quads (chunks that are multiples of 4, aligned arrays) and the
-    one-particle-a-thread push (a chunk that is not) give the same bits: fields, currents (Jz
-    deposited on the last step), probes and particles; on the 1536-cell grid the push launches
-    carry the previous step's H phase."""
+def test_push_chunk_changes_no_bits(nz, clo, chi):
+    """The FP32 push with the default particles-per-CTA and with 1022 (a ragged split of the
+    warps' particles) gives the same bits: fields, currents (Jz deposited on the last step),
+    probes and particles, since deposits are integer sums whose grouping does not matter; on
+    the 1536-cell grid the push launches carry the previous step's H phase."""
     torch = _torch()
     import scipy.constants as sc
     from fdtdpic.grid import lorentz_kerr_grid
@@ -169,7 +169,7 @@ def test_quad_push_equals_scalar_push_bitwise(nz, clo, chi):
     out = []
     for chunk in (0, 1022):
         g = lorentz_kerr_grid(nz, T, front=300, rear=400, nzsrc=60, probes=(50, 350), chi3=1e-2)
-        beam = make_beam(NPART + 3, clo, chi, DZ)  # a ragged last quad
+        beam = make_beam(NPART + 3, clo, chi, DZ)  # a ragged last warp
         run = PicRun(g, beam, DZ, DT, sc.mu_0, precision="f32", chunk=chunk, path="streaming")
         run.step(T)
         torch.cuda.synchronize()
