@@ -570,29 +570,73 @@ __device__ __forceinline__ void push_deposit_jx(unsigned long long *win, const P
     constexpr int W = Fix<T>::W;
     if (!__any_sync(0xffffffffu, jx0 != T(0) || jx1 != T(0))) return;
     const int nx1 = nx0 >= 0 ? nx0 + 1 : -1;
-    // the whole warp on one node pair (a dense beam after re-binning): warp sums
+    if constexpr (sizeof(T) == 4) {
+        // A re-binned dense beam: the warp's particles sit in one or two cells, so their left
+        // nodes nx0 span m .. m + D with D <= 2 and the warp touches nodes m .. m + D + 1.  Node
+        // m + k takes jx0 from the lanes with nx0 = m + k and jx1 from those with nx0 = m + k - 1,
+        // one term per lane, so each node's sum is one warp reduction of a per-lane value.  The
+        // integers are Fix<float>::split's (rint of v * 2^S): below 2^26 one reduction per node
+        // (32 of them sum exactly in 32 bits); below 2^46 two, of the 22-bit low pieces and the
+        // high parts.  Lane k adds node m + k's sum to the window.  Integer sums: the same bits
+        // as the general path below.
+        const bool has = nx0 >= 0;
+        const int m = __reduce_min_sync(0xffffffffu, has ? nx0 : INT_MAX);
+        const int d = has ? nx0 - m : -4;
+        int D = __reduce_max_sync(0xffffffffu, has ? d : 0);
+        const int r0 = m - base;
+        if (D <= 2 && r0 >= 0 && r0 + D + 1 < PIC_WIN) {
+            const float x0 = rintf(jx0 * a.jscale_f), x1 = rintf(jx1 * a.jscale_f);
+            const float ax = fmaxf(fabsf(x0), fabsf(x1));
+            long long s[4] = {0, 0, 0, 0};
+            if (__all_sync(0xffffffffu, ax < 67108864.f)) {  // 2^26
+                const int X0 = __float2int_rn(x0), X1 = __float2int_rn(x1);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (k <= D + 1)
+                        s[k] = __reduce_add_sync(0xffffffffu, d == k ? X0 : (d == k - 1 ? X1 : 0));
+            } else if (__all_sync(0xffffffffu, ax < 70368744177664.f)) {  // 2^46
+                const float h0 = floorf(x0 * 2.384185791015625e-07f);  // x / 2^22
+                const float h1 = floorf(x1 * 2.384185791015625e-07f);
+                const int H0 = __float2int_rn(h0), H1 = __float2int_rn(h1);
+                const unsigned L0 = __float2uint_rn(fmaf(-h0, 4194304.f, x0));  // exact, < 2^22
+                const unsigned L1 = __float2uint_rn(fmaf(-h1, 4194304.f, x1));
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (k <= D + 1) {
+                        const int hs = __reduce_add_sync(
+                            0xffffffffu, d == k ? H0 : (d == k - 1 ? H1 : 0));
+                        const unsigned ls = __reduce_add_sync(
+                            0xffffffffu, d == k ? L0 : (d == k - 1 ? L1 : 0u));
+                        s[k] = (long long)hs * 4194304 + (long long)ls;
+                    }
+            } else {
+                D = 99;  // the general path
+            }
+            if (D <= 2) {
+                const long long v = lane == 0 ? s[0] : lane == 1 ? s[1] : lane == 2 ? s[2] : s[3];
+                if (lane <= D + 1 && v != 0) smem_add_u64(win + r0 + lane, (unsigned long long)v);
+                return;
+            }
+        }
+        // A sparse beam (a few particles a cell: the warp spreads over more nodes than it has
+        // lanes a node): every node inside the window, each lane adds its own two words.
+        if (D < 99 && D > 2 && r0 >= 0 && r0 + D + 1 < PIC_WIN) {
+            if (has) {
+                long long v0, v1;
+                Fix<T>::split(jx0, a.jscale, a.jscale_f, &v0);
+                Fix<T>::split(jx1, a.jscale, a.jscale_f, &v1);
+                if (v0 != 0) smem_add_u64(win + (nx0 - base), (unsigned long long)v0);
+                if (v1 != 0) smem_add_u64(win + (nx0 + 1 - base), (unsigned long long)v1);
+            }
+            return;
+        }
+    }
+    // the whole warp on one node pair: warp sums
     const int i0 = __shfl_sync(0xffffffffu, nx0, 0);
     const int r0 = i0 - base;
     const bool pair =
         __all_sync(0xffffffffu, nx0 == i0) && i0 >= 0 && r0 >= 0 && r0 + 1 < PIC_WIN;
-    bool done = false;
-    if constexpr (sizeof(T) == 4) {
-        // FP32 words below 2^26 (Fix<float>::split's one-conversion case, the same
-        // integers): 32 of them sum exactly in 32 bits, one reduction per node
-        if (pair) {
-            const float x0 = jx0 * a.jscale_f, x1 = jx1 * a.jscale_f;
-            if (__all_sync(0xffffffffu, fabsf(x0) < 67108864.f && fabsf(x1) < 67108864.f)) {
-                const int s0 = __reduce_add_sync(0xffffffffu, __float2int_rn(x0));
-                const int s1 = __reduce_add_sync(0xffffffffu, __float2int_rn(x1));
-                if (lane == 0) {
-                    if (s0 != 0) smem_add_u64(win + r0, (unsigned long long)(long long)s0);
-                    if (s1 != 0) smem_add_u64(win + r0 + 1, (unsigned long long)(long long)s1);
-                }
-                done = true;
-            }
-        }
-    }
-    if (!done) {
+    {
         long long vx0[W], vx1[W];
 #pragma unroll
         for (int w = 0; w < W; ++w) vx0[w] = vx1[w] = 0;
