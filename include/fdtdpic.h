@@ -54,7 +54,8 @@ typedef struct CUstream_st *fdtdpic_stream_t; /* == cudaStream_t */
 #define FDTD_STATUS_NONFINITE 1 /* Ex or Hy not finite at the end of the call */
 #define FDTD_STATUS_SKIPPED 2   /* instance larger than smem_bytes: not run */
 #define FDTD_STATUS_TIMEOUT 4   /* beam step, tiled path: a bounded wait gave up */
-#define FDTD_STATUS_OVERFLOW 8  /* beam step, tiled path: a tile or migrant buffer overflowed */
+#define FDTD_STATUS_OVERFLOW 8  /* beam step, tiled or pass path: a tile, migrant or segment
+                                   buffer overflowed */
 #define FDTD_STATUS_BOUNDS 16   /* the index-checking debug build (libfdtdpic_bounds.so) found an
                                    index outside its buffer and skipped the access */
 
@@ -222,7 +223,12 @@ typedef struct PicBeam {
     int32_t chunk;      /* particles per CTA in the push kernel (0: library default) */
     int32_t path;       /* 0: automatic (= streaming, measured faster on GB300 at every size
                            but the smallest, where the two tie), 1: streaming kernels,
-                           2: persistent tiled kernel; may be or-ed with
+                           2: persistent tiled kernel, 3: temporally blocked passes (long
+                           grids: sort_every whole steps per launch, 0 for 8, over tiles of
+                           about chunk cells, 0 for 512, each tile's fields and particles in
+                           shared memory; needs FDTDPIC_PATH_CELLS_INSIDE, else
+                           FDTDPIC_ERR_ARG, as for tiles narrower than twice the pass's halo
+                           of 3 sort_every + 4 cells); may be or-ed with
                            FDTDPIC_PATH_CELLS_INSIDE */
     double kE;     /* q dt / (2 m c) */
     double kH;     /* -q mu0 dt / (2 m) */
@@ -242,15 +248,17 @@ typedef struct FdtdPicTiming {
     float sort_ms;  /* re-binning by cell */
     int32_t steps;
     int32_t path;   /* 1: streaming kernels, 2: persistent tiled kernel (push_ms = whole kernel),
-                       3: streaming kernels, each push launch carrying the previous H phase */
+                       3: streaming kernels, each push launch carrying the previous H phase,
+                       4: temporally blocked passes (push_ms = all passes) */
 } FdtdPicTiming;
 
 /* Bytes of caller scratch fdtdpic_run needs (deposit accumulators, re-binning buffers). */
 int64_t fdtdpic_scratch_bytes(int precision, int nz, int n_part);
 /* Bytes of scratch fdtdpic_run needs for this run on the current device: for beam->path == 2
  * the persistent tiled path's requirement (the tiled path applies when the grid splits into at
- * least two tiles of >= max(pml+2, 8) cells, one per SM, each fitting shared memory), else the
- * streaming path's. */
+ * least two tiles of >= max(pml+2, 8) cells, one per SM, each fitting shared memory); for
+ * path 3 (with FDTDPIC_PATH_CELLS_INSIDE) the temporally blocked path's (its particle segments,
+ * double buffered, and a second copy of the state and of Hyp); else the streaming path's. */
 int64_t fdtdpic_pic_scratch_bytes(int precision, const FdtdInstance *inst, const PicBeam *beam);
 /* The largest power-of-two scale for which no deposit accumulator can overflow. */
 double fdtdpic_pic_jscale(const PicBeam *beam);

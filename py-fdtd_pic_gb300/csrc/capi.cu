@@ -6,7 +6,7 @@
 
 #include "fdtd1d_launch.cuh"
 #include "pic_kernel.cuh"
-#include "pic_tiled.cuh"
+#include "pic_pass.cuh"
 
 #include <atomic>
 
@@ -48,6 +48,29 @@ int run_pic_tiled_f32(const FdtdInstance &h, const BatchArgs<float> &fa, const P
                       const TileGeom &g, int32_t *cell, float *frac, float *ux, float *uz,
                       int32_t *id, float *jx, float *jz, float *hyp, unsigned char *scratch,
                       int32_t *status, FdtdPicTiming *timing, cudaStream_t st);
+
+int run_pic_pass_f64(const FdtdInstance &h, const BatchArgs<double> &fa, const PicBeam &bm,
+                     const PassGeom &g, int32_t *cell, double *frac, double *ux, double *uz,
+                     int32_t *id, double *jx, double *jz, double *hyp, unsigned char *scratch,
+                     int32_t *status, FdtdPicTiming *timing, cudaStream_t st);
+int run_pic_pass_f32(const FdtdInstance &h, const BatchArgs<float> &fa, const PicBeam &bm,
+                     const PassGeom &g, int32_t *cell, float *frac, float *ux, float *uz,
+                     int32_t *id, float *jx, float *jz, float *hyp, unsigned char *scratch,
+                     int32_t *status, FdtdPicTiming *timing, cudaStream_t st);
+
+// Geometry of the temporally blocked path (path mode 3) on the current device, or ok=false when
+// it does not apply (the beam must also be inside its domain: FDTDPIC_PATH_CELLS_INSIDE).
+static PassGeom pass_geometry_dev(int precision, const FdtdInstance &h, const PicBeam &b)
+{
+    PassGeom g{};
+    int dev = 0, max_optin = 0;
+    if ((b.path & FDTDPIC_PATH_MODE) != 3 || !(b.path & FDTDPIC_PATH_CELLS_INSIDE) ||
+        cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+            cudaSuccess)
+        return g;
+    return pass_geometry(precision, h, b, max_optin);
+}
 
 // Tiling of a beam run on the current device, or ok=false when the tiled path does not apply
 // (fewer than two tiles of the minimum width, or a tile's fields beyond shared memory).
@@ -264,6 +287,8 @@ int64_t fdtdpic_pic_scratch_bytes(int precision, const FdtdInstance *inst, const
     if (!inst || !beam || (precision != FDTDPIC_F64 && precision != FDTDPIC_F32)) return 0;
     if (check_instance(*inst) != FDTDPIC_OK) return 0;
     int64_t need = fdtdpic_scratch_bytes(precision, inst->nz, beam->n_part);
+    const PassGeom pg = pass_geometry_dev(precision, *inst, *beam);
+    if (pg.ok) return (int64_t)pass_scratch_layout(precision, inst->nz, pg).total;
     const TileGeom tg = tiled_geometry(precision, *inst, *beam);
     if (tg.ok) {
         const int64_t t = (int64_t)tile_scratch_layout(precision, tg).total;
@@ -293,10 +318,28 @@ int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d
     if (b.n_part > 0 && (!d_cell || !d_frac || !d_ux || !d_uz || !d_id)) return FDTDPIC_ERR_ARG;
     if (precision != FDTDPIC_F64 && precision != FDTDPIC_F32) return FDTDPIC_ERR_ARG;
     if ((b.path & ~(FDTDPIC_PATH_MODE | FDTDPIC_PATH_CELLS_INSIDE)) != 0 ||
-        (b.path & FDTDPIC_PATH_MODE) > 2)
+        (b.path & FDTDPIC_PATH_MODE) > 3)
         return FDTDPIC_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     unsigned char *scr = (unsigned char *)d_scratch;
+    if ((b.path & FDTDPIC_PATH_MODE) == 3) {
+        const PassGeom pg = pass_geometry_dev(precision, *h_inst, b);
+        if (!pg.ok) return FDTDPIC_ERR_ARG;
+        if (scratch_bytes < (int64_t)pass_scratch_layout(precision, h_inst->nz, pg).total)
+            return FDTDPIC_ERR_OOM;
+        if (precision == FDTDPIC_F64) {
+            BatchArgs<double> a{1, d_inst, nullptr, d_pml_tab, d_src, (double *)d_state,
+                                (double *)d_probe, nullptr, nullptr, nullptr, nullptr, 0};
+            return run_pic_pass_f64(*h_inst, a, b, pg, d_cell, (double *)d_frac, (double *)d_ux,
+                                    (double *)d_uz, d_id, (double *)d_jx, (double *)d_jz,
+                                    (double *)d_hyp, scr, d_status, timing, st);
+        }
+        BatchArgs<float> a{1, d_inst, nullptr, d_pml_tab, d_src, (float *)d_state,
+                           (float *)d_probe, nullptr, nullptr, nullptr, nullptr, 0};
+        return run_pic_pass_f32(*h_inst, a, b, pg, d_cell, (float *)d_frac, (float *)d_ux,
+                                (float *)d_uz, d_id, (float *)d_jx, (float *)d_jz,
+                                (float *)d_hyp, scr, d_status, timing, st);
+    }
     const TileGeom tg = tiled_geometry(precision, *h_inst, b);
     const int64_t tiled_need = tg.ok ? (int64_t)tile_scratch_layout(precision, tg).total : -1;
     if (tg.ok && scratch_bytes >= tiled_need) {

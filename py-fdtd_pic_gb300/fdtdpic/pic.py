@@ -103,11 +103,14 @@ class PicRun:
     """One grid plus a beam, resident on the GPU; ``step(n)`` advances n steps.
 
     path: "auto" (the streaming kernels: push, field and re-binning launches captured in CUDA
-    graphs; measured faster than the persistent tiled kernel on GB300), "streaming" or "tiled"
-    (one cooperative launch for all steps; grids that tile over the SMs only)."""
+    graphs; measured faster than the persistent tiled kernel on GB300), "streaming", "tiled"
+    (one cooperative launch for all steps; grids that tile over the SMs only) or "pass" (long
+    grids: pass_steps whole steps per launch over tiles of about tile_cells cells held in shared
+    memory; 0 for the library's defaults, 8 steps and 512 cells; beams inside their domain)."""
 
     def __init__(self, grid: Grid, beam: Beam, dz: float, dt: float, mu0: float,
-                 precision="f32", sort_every=32, chunk=0, path="auto", device=None):
+                 precision="f32", sort_every=32, chunk=0, path="auto", device=None,
+                 pass_steps=0, tile_cells=0):
         _require_cuda()
         self.L = lib()
         self.prec, self.tdt = _dtype(precision)
@@ -136,11 +139,13 @@ class PicRun:
         self.pb = PicBeam()
         self.pb.n_part, self.pb.clo, self.pb.chi = beam.n, beam.clo, beam.chi
         self.pb.sort_every, self.pb.chunk = sort_every, chunk
+        if path == "pass":  # the pass path reads these two fields as its pass length and tiles
+            self.pb.sort_every, self.pb.chunk = pass_steps, tile_cells
         self.constants = beam_constants(dz, dt, beam.weight, mu0)
         for name, v in self.constants.items():
             setattr(self.pb, name, v)
         self.pb.jscale = self.L.fdtdpic_pic_jscale(ctypes.byref(self.pb))
-        self.path_mode = {"auto": 0, "streaming": 1, "tiled": 2}[path]
+        self.path_mode = {"auto": 0, "streaming": 1, "tiled": 2, "pass": 3}[path]
         self._set_inside(beam)
         self.scratch_bytes = int(self.L.fdtdpic_pic_scratch_bytes(
             self.prec, self.desc.ctypes.data, ctypes.byref(self.pb)))
@@ -269,7 +274,7 @@ class PicRun:
 
 
 def large_case(nz=1 << 24, n_part=64 << 20, total=20000, dz=0.015, nzsrc=100, precision="f32",
-               sort_every=32, path="auto", chunk=0):
+               sort_every=32, path="auto", chunk=0, pass_steps=0, tile_cells=0):
     """The large single-instance workload: ``nz`` cells, ``n_part`` macroparticles spread over
     the whole grid, a Kerr slab over the middle half, ``total`` steps (at the default sizes:
     2^24 cells, 64M particles, 20,000 steps, FP32)."""
@@ -280,7 +285,8 @@ def large_case(nz=1 << 24, n_part=64 << 20, total=20000, dz=0.015, nzsrc=100, pr
                           probes=(50, nz - 50), chi3=1e-2)
     beam = make_beam(n_part, 50, nz - 51, dz, seed=7, sort=False)
     return PicRun(g, beam, dz, 0.5 * dz / C0, sc.mu_0, precision=precision,
-                  sort_every=sort_every, chunk=chunk, path=path)
+                  sort_every=sort_every, chunk=chunk, path=path, pass_steps=pass_steps,
+                  tile_cells=tile_cells)
 
 
 def _main(argv=None):
@@ -295,11 +301,14 @@ def _main(argv=None):
     ap.add_argument("--steps", type=int, default=256)
     ap.add_argument("--warmup", type=int, default=64)
     ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
-    ap.add_argument("--path", choices=["auto", "streaming", "tiled"], default="auto")
+    ap.add_argument("--path", choices=["auto", "streaming", "tiled", "pass"], default="auto")
     ap.add_argument("--chunk", type=int, default=0, help="particles per push CTA (0: default)")
+    ap.add_argument("--pass-steps", type=int, default=0, help="pass path: steps a launch")
+    ap.add_argument("--tile-cells", type=int, default=0, help="pass path: cells a tile")
     a = ap.parse_args(argv)
     run = large_case(a.nz, a.particles, a.warmup + 2 * a.steps, precision=a.precision,
-                     path=a.path, chunk=a.chunk)
+                     path=a.path, chunk=a.chunk, pass_steps=a.pass_steps,
+                     tile_cells=a.tile_cells)
     run.step(a.warmup)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
