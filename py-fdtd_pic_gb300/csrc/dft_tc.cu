@@ -7,19 +7,24 @@
 // fdtdpic_dft_probes).  Each operand is split into two BF16 halves, x = xh + xl and
 // B = Bh + Bl (xl = bf16(x - xh)), and C ~= xh Bh + xh Bl + xl Bh: three BF16 MMAs per K step,
 // about 16 significant bits per product, FP32 sums in tensor memory over TC_FLUSH chunks of
-// TC_KC steps, then compensated FP32 sums (a float pair per output, error-free two-sum) in
-// shared memory: the group sums' rounding is bounded by one flush group of 1024 steps, and the
+// TC_KC steps, then compensated FP32 sums (a float pair per output, error-free two-sum), also in
+// tensor memory: the group sums' rounding is bounded by one flush group of 1024 steps, and the
 // sums across groups keep ~48 bits without the narrow FP64 pipe.
 //
 // Three launches:
 //   dft_tc_pack_traces   traces -> BF16 hi/lo operand tiles, one 32 KiB block per (128 traces,
 //                        64 steps), already in the MMA's shared-memory layout (canonical
 //                        no-swizzle K-major: 8-row x 16-byte core matrices)
-//   dft_tc_pack_twiddles twiddle table -> 16 KiB blocks per (32 frequencies x re/im, 64 steps)
-//   dft_tc_kernel        one CTA per 128-trace x 64-column tile: a two-stage pipeline of bulk
-//                        asynchronous copies (cp.async.bulk, mbarrier transaction counts) feeding
-//                        the tensor cores; one thread issues the 12 MMAs of a chunk and commits
-//                        them to an mbarrier; every wait is bounded.
+//   dft_tc_pack_twiddles twiddle table -> 32 KiB blocks per (64 frequencies x re/im, 64 steps)
+//   dft_tc_kernel        one CTA per 128-trace x 128-column tile, warp-specialised: a producer
+//                        thread streams the chunks' operand blocks through a three-stage ring
+//                        of bulk asynchronous copies (cp.async.bulk, mbarrier transaction
+//                        counts); an MMA thread issues each chunk's 12 MMAs as soon as its
+//                        stage is full and frees the stage with a commit, never waiting for
+//                        the MMAs themselves; the flush groups alternate between two tensor-
+//                        memory accumulators, so four epilogue warps fold one group into the
+//                        compensated sums while the tensor cores fill the other.  Every wait
+//                        is bounded.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -32,22 +37,24 @@ namespace fdtdpic {
 int cuda_status(cudaError_t e);
 
 constexpr int TC_M = 128;          // traces per CTA = MMA M = tensor memory lanes
-constexpr int TC_N = 64;           // output columns per CTA (32 frequencies x re/im) = MMA N
+constexpr int TC_N = 128;          // output columns per CTA (64 frequencies x re/im) = MMA N
 constexpr int TC_Q = TC_N / 2;     // frequencies per CTA
 constexpr int TC_KC = 64;          // time steps per chunk (one pipeline stage)
 constexpr int TC_KSTEP = 16;       // K of one kind::f16 MMA
 constexpr int TC_FLUSH = 16;       // chunks summed in FP32 before the compensated sums
-constexpr int TC_THREADS = 128;
-constexpr int TC_TMEM_COLS = 64;   // FP32 accumulator columns (power of two >= 32)
+constexpr int TC_STAGES = 3;
+constexpr int TC_EPI_WARPS = 4;    // epilogue warps: warp w reads tensor memory lanes 32w ..
+constexpr int TC_THREADS = 32 * (TC_EPI_WARPS + 2);  // + the producer warp and the MMA warp
+constexpr int TC_TMEM_COLS = 512;  // accumulators [0, 2N), sums [2N, 3N), errors [3N, 4N)
 constexpr uint32_t TC_LBO = 128;                          // next core matrix along K
 constexpr uint32_t TC_SBO = (TC_KC / 8) * 128;            // next 8 rows: 1024 B
 constexpr uint32_t TC_A_HALF = (TC_M / 8) * TC_SBO;        // 16 KiB
-constexpr uint32_t TC_B_HALF = (TC_N / 8) * TC_SBO;        // 8 KiB
+constexpr uint32_t TC_B_HALF = (TC_N / 8) * TC_SBO;        // 16 KiB
 constexpr uint32_t TC_A_BLOCK = 2 * TC_A_HALF;             // hi then lo
 constexpr uint32_t TC_B_BLOCK = 2 * TC_B_HALF;
-constexpr uint32_t TC_STAGE = TC_A_BLOCK + TC_B_BLOCK;     // 48 KiB
-constexpr uint32_t TC_ACC_BYTES = TC_M * TC_N * 8;         // float-pair tile, 64 KiB
-constexpr uint32_t TC_SMEM = 2 * TC_STAGE + TC_ACC_BYTES + 64;
+constexpr uint32_t TC_STAGE = TC_A_BLOCK + TC_B_BLOCK;     // 64 KiB
+constexpr int TC_BARS = 2 * TC_STAGES + 4;                 // full, empty, accfull, accempty
+constexpr uint32_t TC_SMEM = TC_STAGES * TC_STAGE + 8 * TC_BARS + 16;
 
 // Byte offset of element (row, k) of a K-major operand tile in the core-matrix layout.
 __host__ __device__ __forceinline__ uint32_t tc_off(int row, int k)
@@ -179,28 +186,66 @@ __global__ void dft_tc_pack_twiddles(const float2 *tw, int F, int S, int n_kc, i
     }
 }
 
+__device__ __forceinline__ void tc_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+        bar));
+}
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&v)[16])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+        "%14,%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+          "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
+}
+
+__device__ __forceinline__ void tc_st16(uint32_t taddr, const uint32_t (&v)[16])
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+        "%13,%14,%15,%16};" ::"r"(taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+        "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
+        "r"(v[15])
+        : "memory");
+}
+
+// Barriers (mbarrier phases): full[s] completes when stage s's copies land (the j-th time:
+// chunk s + 3j), empty[s] when the MMAs reading it complete (chunk s + 3j), accfull[b] when the
+// MMAs of flush group b + 2j complete, accempty[b] when the epilogue has read group b + 2j.
 __global__ void __launch_bounds__(TC_THREADS, 1)
     dft_tc_kernel(const unsigned char *a_tiles, const unsigned char *b_tiles, int n_kc, int R,
                   int F, double *out, int32_t *err)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
-    float2 *acc = reinterpret_cast<float2 *>(sm + 2 * TC_STAGE);  // [TC_N][TC_M] (sum, error)
-    uint64_t *bars = reinterpret_cast<uint64_t *>(acc + TC_M * TC_N);  // full[0], full[1], mma
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 3);
-    const int tid = threadIdx.x, warp = tid >> 5;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + TC_STAGES * TC_STAGE);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + TC_BARS);
+    __shared__ int s_abort, s_loads, s_mmas;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ct = blockIdx.x, rt = blockIdx.y;
     const int r0 = rt * TC_M, q0 = ct * TC_Q;
     const unsigned char *a_src = a_tiles + (int64_t)rt * n_kc * TC_A_BLOCK;
     const unsigned char *b_src = b_tiles + (int64_t)ct * n_kc * TC_B_BLOCK;
-
-    for (int i = tid; i < TC_M * TC_N; i += TC_THREADS) acc[i] = make_float2(0.f, 0.f);
     const uint32_t s_base = (uint32_t)__cvta_generic_to_shared(sm);
-    const uint32_t full0 = (uint32_t)__cvta_generic_to_shared(bars);
-    const uint32_t mma_bar = full0 + 16;
+    const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(bars);
+    auto full_bar = [&](int st) { return bar0 + 8u * (uint32_t)st; };
+    auto empty_bar = [&](int st) { return bar0 + 8u * (uint32_t)(TC_STAGES + st); };
+    auto accfull_bar = [&](int b) { return bar0 + 8u * (uint32_t)(2 * TC_STAGES + b); };
+    auto accempty_bar = [&](int b) { return bar0 + 8u * (uint32_t)(2 * TC_STAGES + 2 + b); };
     if (tid == 0) {
-        for (int b = 0; b < 3; ++b)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0 + 8 * b));
+        for (int i = 0; i < 2 * TC_STAGES + 2; ++i)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8u * (uint32_t)i));
+        for (int b = 0; b < 2; ++b)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(accempty_bar(b)),
+                         "r"(32 * TC_EPI_WARPS));
         asm volatile("fence.mbarrier_init.release.cluster;");
+        s_abort = 0;
+        s_loads = 0;
+        s_mmas = 0;
     }
     if (warp == 0) {
         const uint32_t slot_a = (uint32_t)__cvta_generic_to_shared(tmem_slot);
@@ -212,90 +257,131 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = *tmem_slot;
-    const uint32_t t_row = tmem + ((uint32_t)(warp * 32) << 16);  // lanes 32w..32w+31
+    const int n_groups = (n_kc + TC_FLUSH - 1) / TC_FLUSH;
 
-    auto issue_loads = [&](int c) {
-        const uint32_t st = s_base + (uint32_t)(c & 1) * TC_STAGE;
-        const uint32_t bar = full0 + 8u * (uint32_t)(c & 1);
-        tc_expect(bar, TC_STAGE);
-        tc_bulk_load(st, a_src + (int64_t)c * TC_A_BLOCK, TC_A_BLOCK, bar);
-        tc_bulk_load(st + TC_A_BLOCK, b_src + (int64_t)c * TC_B_BLOCK, TC_B_BLOCK, bar);
-    };
-    if (tid == 0) issue_loads(0);
-
-    bool ok = true;
-    int issued = 1;      // chunks whose loads were issued
-    int mma_issued = 0;  // chunks whose MMAs were issued
-    for (int c = 0; c < n_kc; ++c) {
-        const int s = c & 1;
-        if (tid == 0 && c + 1 < n_kc) {  // the other stage was freed by chunk c-1's MMAs
-            issue_loads(c + 1);
-        }
-        if (c + 1 < n_kc) issued = c + 2;
-        if (!__syncthreads_and((int)tc_wait(full0 + 8u * s, (uint32_t)((c >> 1) & 1)))) {
-            ok = false;
-            break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        if (tid == 0) {
-            const uint32_t a_hi = s_base + (uint32_t)s * TC_STAGE, a_lo = a_hi + TC_A_HALF;
-            const uint32_t b_hi = a_hi + TC_A_BLOCK, b_lo = b_hi + TC_B_HALF;
-            const bool fresh = (c % TC_FLUSH) == 0;
-#pragma unroll
-            for (int k = 0; k < TC_KC / TC_KSTEP; ++k) {
-                const uint32_t ko = (uint32_t)k * 2 * TC_LBO;  // two core matrices per K step
-                tc_mma(tmem, tc_desc(a_hi + ko), tc_desc(b_hi + ko), (fresh && k == 0) ? 0u : 1u);
-                tc_mma(tmem, tc_desc(a_hi + ko), tc_desc(b_lo + ko), 1u);
-                tc_mma(tmem, tc_desc(a_lo + ko), tc_desc(b_hi + ko), 1u);
+    if (warp == TC_EPI_WARPS) {
+        // producer: chunk c into stage c % 3 once the MMAs of chunk c - 3 have freed it
+        if (lane == 0) {
+            for (int c = 0; c < n_kc; ++c) {
+                const int st = c % TC_STAGES, k = c / TC_STAGES;
+                if (k > 0 && !tc_wait(empty_bar(st), (uint32_t)((k - 1) & 1))) {
+                    atomicOr(&s_abort, 1);
+                    break;
+                }
+                if (*(volatile int *)&s_abort) break;
+                const uint32_t dst = s_base + (uint32_t)st * TC_STAGE;
+                tc_expect(full_bar(st), TC_STAGE);
+                tc_bulk_load(dst, a_src + (int64_t)c * TC_A_BLOCK, TC_A_BLOCK, full_bar(st));
+                tc_bulk_load(dst + TC_A_BLOCK, b_src + (int64_t)c * TC_B_BLOCK, TC_B_BLOCK,
+                             full_bar(st));
+                s_loads = c + 1;
             }
-            asm volatile(
-                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                    mma_bar));
         }
-        mma_issued = c + 1;
-        if (!__syncthreads_and((int)tc_wait(mma_bar, (uint32_t)(c & 1)))) {
-            ok = false;
-            break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        if ((c % TC_FLUSH) == TC_FLUSH - 1 || c == n_kc - 1) {
-            // this thread's row of the FP32 accumulator -> the compensated sums
+    } else if (warp == TC_EPI_WARPS + 1) {
+        // MMA issuer: chunk c's 12 MMAs into accumulator (c / TC_FLUSH) % 2 as soon as its stage
+        // is full; a commit frees the stage, another after a group's last chunk hands the
+        // accumulator to the epilogue
+        if (lane == 0) {
+            for (int c = 0; c < n_kc; ++c) {
+                const int st = c % TC_STAGES, k = c / TC_STAGES;
+                const int g = c / TC_FLUSH, b = g & 1;
+                const bool first = (c % TC_FLUSH) == 0;
+                const bool last = (c % TC_FLUSH) == TC_FLUSH - 1 || c == n_kc - 1;
+                if (first && g >= 2 &&
+                    !tc_wait(accempty_bar(b), (uint32_t)(((g >> 1) - 1) & 1))) {
+                    atomicOr(&s_abort, 1);
+                    break;
+                }
+                if (!tc_wait(full_bar(st), (uint32_t)(k & 1))) {
+                    atomicOr(&s_abort, 1);
+                    break;
+                }
+                if (*(volatile int *)&s_abort) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t a_hi = s_base + (uint32_t)st * TC_STAGE, a_lo = a_hi + TC_A_HALF;
+                const uint32_t b_hi = a_hi + TC_A_BLOCK, b_lo = b_hi + TC_B_HALF;
+                const uint32_t d = tmem + (uint32_t)(b * TC_N);
 #pragma unroll
+                for (int kk = 0; kk < TC_KC / TC_KSTEP; ++kk) {
+                    const uint32_t ko = (uint32_t)kk * 2 * TC_LBO;  // two core matrices per K step
+                    tc_mma(d, tc_desc(a_hi + ko), tc_desc(b_hi + ko), (first && kk == 0) ? 0u : 1u);
+                    tc_mma(d, tc_desc(a_hi + ko), tc_desc(b_lo + ko), 1u);
+                    tc_mma(d, tc_desc(a_lo + ko), tc_desc(b_hi + ko), 1u);
+                }
+                tc_commit(empty_bar(st));
+                if (last) tc_commit(accfull_bar(b));
+                s_mmas = c + 1;
+            }
+        }
+    } else {
+        // epilogue: each thread one trace (tensor memory lane 32 warp + lane); per group, the
+        // FP32 accumulator folded into the (sum, error) pairs by an error-free two-sum; the last
+        // group's pairs go out as sum + error in FP64
+        const uint32_t t_lane = tmem + ((uint32_t)(warp * 32) << 16);
+        const int r = r0 + warp * 32 + lane;
+        for (int g = 0; g < n_groups; ++g) {
+            const int b = g & 1;
+            if (!tc_wait(accfull_bar(b), (uint32_t)((g >> 1) & 1))) {
+                atomicOr(&s_abort, 1);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const bool fin = g == n_groups - 1;
+#pragma unroll 1
             for (int c0 = 0; c0 < TC_N; c0 += 16) {
-                uint32_t v[16];
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,"
-                    "%11,%12,%13,%14,%15}, [%16];"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-                      "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-                      "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-                    : "r"(t_row + (uint32_t)c0));
-                asm volatile("tcgen05.wait::ld.sync.aligned;");
+                uint32_t v[16], su[16], er[16];
+                tc_ld16(t_lane + (uint32_t)(b * TC_N + c0), v);
+                if (g > 0) {
+                    tc_ld16(t_lane + (uint32_t)(2 * TC_N + c0), su);
+                    tc_ld16(t_lane + (uint32_t)(3 * TC_N + c0), er);
+                }
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                    float2 &a2 = acc[(c0 + j) * TC_M + tid];
-                    const float b = __uint_as_float(v[j]);
-                    const float s2 = __fadd_rn(a2.x, b);  // two-sum: s2 + e == a2.x + b exactly
-                    const float bp = __fsub_rn(s2, a2.x);
-                    const float e = __fadd_rn(__fsub_rn(a2.x, __fsub_rn(s2, bp)), __fsub_rn(b, bp));
-                    a2.x = s2;
-                    a2.y = __fadd_rn(a2.y, e);
+                    const float x = __uint_as_float(v[j]);
+                    float sum = x, e = 0.f;
+                    if (g > 0) {
+                        const float a0 = __uint_as_float(su[j]);
+                        sum = __fadd_rn(a0, x);  // two-sum: sum + t == a0 + x exactly
+                        const float bp = __fsub_rn(sum, a0);
+                        const float t = __fadd_rn(__fsub_rn(a0, __fsub_rn(sum, bp)),
+                                                  __fsub_rn(x, bp));
+                        e = __fadd_rn(__uint_as_float(er[j]), t);
+                    }
+                    su[j] = __float_as_uint(sum);
+                    er[j] = __float_as_uint(e);
+                }
+                if (fin) {
+                    if (r < R)
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const int col = c0 + j, f = q0 + (col >> 1);
+                            if (f < F)
+                                out[((int64_t)r * F + f) * 2 + (col & 1)] =
+                                    (double)__uint_as_float(su[j]) + (double)__uint_as_float(er[j]);
+                        }
+                } else {
+                    tc_st16(t_lane + (uint32_t)(2 * TC_N + c0), su);
+                    tc_st16(t_lane + (uint32_t)(3 * TC_N + c0), er);
                 }
             }
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(accempty_bar(b))
+                         : "memory");
         }
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();  // accumulator read before the next chunk's first MMA
-        asm volatile("tcgen05.fence::after_thread_sync;");
     }
-    if (!ok) {
-        // a wait gave up: record it, then wait (bounded) for every copy and MMA this CTA started
-        // before its shared and tensor memory are released
-        if (tid == 0) {
-            atomicOr(err, 1);
-            for (int c = issued - 2 < 0 ? 0 : issued - 2; c < issued; ++c)  // latest per stage
-                tc_wait(full0 + 8u * (c & 1), (uint32_t)((c >> 1) & 1));
-            if (mma_issued > 0) tc_wait(mma_bar, (uint32_t)((mma_issued - 1) & 1));
-        }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (s_abort && tid == 0) {
+        // a wait gave up: record it, then wait (bounded) for the copies and MMAs this CTA
+        // started before its shared and tensor memory are released
+        atomicOr(err, 1);
+        for (int c = s_loads - TC_STAGES < 0 ? 0 : s_loads - TC_STAGES; c < s_loads; ++c)
+            tc_wait(full_bar(c % TC_STAGES), (uint32_t)((c / TC_STAGES) & 1));
+        for (int c = s_mmas - TC_STAGES < 0 ? 0 : s_mmas - TC_STAGES; c < s_mmas; ++c)
+            tc_wait(empty_bar(c % TC_STAGES), (uint32_t)((c / TC_STAGES) & 1));
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
@@ -303,16 +389,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                      "r"(TC_TMEM_COLS));
-    if (!ok) return;
-    const int r = r0 + tid;
-    if (r < R)
-        for (int c = 0; c < TC_N; ++c) {
-            const int f = q0 + (c >> 1);
-            if (f < F) {
-                const float2 a2 = acc[c * TC_M + tid];
-                out[((int64_t)r * F + f) * 2 + (c & 1)] = (double)a2.x + (double)a2.y;
-            }
-        }
 }
 
 struct TcLayout {
