@@ -69,17 +69,20 @@ __host__ __device__ inline int pass_group_off(int g, int capE, int capM)
     return g == 0 ? 0 : (g == 1 ? capE : capE + capM);
 }
 
-// Shared-memory bytes of one CTA holding NR regions.
-__host__ __device__ inline int64_t pass_smem_bytes(int tsize, int NR, int Lmax, int pcap)
+// Shared-memory bytes of one CTA holding NR regions: currents (Jx, Jz words), Ex, Hy, Hyp, Dx
+// per loaded cell, P and P one step back per loaded cell on Lorentz grids (lin), both psi arrays
+// by PML table column (pw = 2 pml + 1 columns), the particles.
+__host__ __device__ inline int64_t pass_smem_bytes(int tsize, int NR, int Lmax, int pcap, int lin,
+                                                   int pw)
 {
     const int W = (tsize == 8) ? 2 : 1;
     const int64_t LL = (int64_t)NR * Lmax;
-    int64_t b = 2LL * W * LL * 8 + 8LL * LL * tsize;
+    int64_t b = 2LL * W * LL * 8 + (4LL + 2 * lin) * LL * tsize + ((2LL * pw * tsize + 7) & ~7LL);
     b += (int64_t)NR * pcap * (8 + 3 * tsize);
     return (b + 15) & ~15LL;
 }
 
-// The fields of the loaded cells; cell k of region r at k - base[r].
+// The fields of the loaded cells (cell k of region r at k - base[r]); psi by PML table column.
 template <typename T, int NR>
 struct PassStore {
     T *ex, *hy, *dx, *p, *pp, *psie, *psih;
@@ -94,8 +97,8 @@ struct PassStore {
     __device__ T &Dx(int k) { return dx[loc(k)]; }
     __device__ T &P(int k) { return p[loc(k)]; }
     __device__ T &Pp(int k) { return pp[loc(k)]; }
-    __device__ T &PsiE(int, int k) { return psie[loc(k)]; }
-    __device__ T &PsiH(int, int k) { return psih[loc(k)]; }
+    __device__ T &PsiE(int col, int) { return psie[col]; }
+    __device__ T &PsiH(int col, int) { return psih[col]; }
     __device__ T tab_at(int row, int col) const { return (T)tab[row * W + col]; }
 };
 
@@ -137,13 +140,19 @@ __global__ void __launch_bounds__(PASS_THREADS, 2) pic_pass_kernel(PassArgs<T> a
     }
     const int LL = NR * a.Lmax;
 
-    // shared memory: currents [2W][LL] (Jx words, then Jz words), fields [8][LL], particles
+    // shared memory: currents [2W][LL] (Jx words, then Jz words), Ex, Hy, Hyp, Dx [LL] each,
+    // P and P one step back [LL] each on Lorentz grids, psi_e and psi_h by PML column, particles
     unsigned long long *jw = reinterpret_cast<unsigned long long *>(sm_raw);
     T *fl = reinterpret_cast<T *>(jw + (size_t)2 * W * LL);
-    T *ex = fl, *hy = fl + LL, *hyp = fl + 2 * LL, *dx = fl + 3 * LL, *pc = fl + 4 * LL;
-    T *pp = fl + 5 * LL, *psie = fl + 6 * LL, *psih = fl + 7 * LL;
+    T *ex = fl, *hy = fl + LL, *hyp = fl + 2 * LL, *dx = fl + 3 * LL;
+    const int lin = I.mode == FDTD_MODE_LINLOR ? 1 : 0;
+    T *pc = lin ? fl + 4 * LL : ex;  // (never read or written on other grids)
+    T *pp = lin ? fl + 5 * LL : ex;
+    const int pw = 2 * I.pml + 1;
+    T *psie = fl + (4 + 2 * lin) * LL, *psih = psie + pw;
     const int pcap = NR * a.pcap;
-    T *pfrac = fl + 8 * LL;
+    T *pfrac = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(fl) +
+                                     (((4LL + 2 * lin) * LL * sizeof(T) + 2LL * pw * sizeof(T) + 7) & ~7LL));
     T *pux = pfrac + pcap, *puz = pux + pcap;
     int32_t *pcell = reinterpret_cast<int32_t *>(puz + pcap);
     int32_t *pid = pcell + pcap;
@@ -167,10 +176,12 @@ __global__ void __launch_bounds__(PASS_THREADS, 2) pic_pass_kernel(PassArgs<T> a
             hy[l] = gi[(int64_t)FDTD_ST_HY * n + k];
             hyp[l] = a.hyp_in[k];
             dx[l] = u.dx ? gi[(int64_t)FDTD_ST_DX * n + k] : T(0);
-            pc[l] = u.p ? gi[(int64_t)FDTD_ST_P * n + k] : T(0);
-            pp[l] = u.p ? gi[(int64_t)FDTD_ST_PPREV * n + k] : T(0);
-            psie[l] = u.psie ? gi[(int64_t)FDTD_ST_PSIE * n + k] : T(0);
-            psih[l] = u.psih ? gi[(int64_t)FDTD_ST_PSIH * n + k] : T(0);
+            if (lin) {
+                pc[l] = u.p ? gi[(int64_t)FDTD_ST_P * n + k] : T(0);
+                pp[l] = u.p ? gi[(int64_t)FDTD_ST_PPREV * n + k] : T(0);
+            }
+            if (u.psie) psie[pml_col(I, k)] = gi[(int64_t)FDTD_ST_PSIE * n + k];
+            if (u.psih) psih[pml_col(I, k)] = gi[(int64_t)FDTD_ST_PSIH * n + k];
 #pragma unroll
             for (int w = 0; w < 2 * W; ++w) jw[(size_t)w * LL + l] = 0ull;
         }
@@ -216,17 +227,32 @@ __global__ void __launch_bounds__(PASS_THREADS, 2) pic_pass_kernel(PassArgs<T> a
     }
     __syncthreads();
     const int np = s_np;
+    // four particles a thread per round, their loads issued before any store
     for (int q = 0; q < s_nsrc; ++q) {
-        const int o0 = s_src_off[q], cnt = s_src_off[q + 1] - o0;
+        const int o0 = s_src_off[q], cnt = min(s_src_off[q + 1], pcap) - o0;
         const long long at = s_src_at[q];
-        for (int i = tid; i < cnt; i += nt) {
-            const int d = o0 + i;
-            if (d >= pcap) break;
-            pcell[d] = a.cell_in[at + i];
-            pfrac[d] = a.frac_in[at + i];
-            pux[d] = a.ux_in[at + i];
-            puz[d] = a.uz_in[at + i];
-            pid[d] = a.id_in[at + i];
+        for (int i0 = 0; i0 < cnt; i0 += 4 * nt) {
+            int c4[4], d4[4];
+            T f4[4], x4[4], z4[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int i = i0 + u * nt + tid;
+                const bool in = i < cnt;
+                const long long g = at + (in ? i : 0);
+                c4[u] = in ? a.cell_in[g] : 0;
+                f4[u] = in ? a.frac_in[g] : T(0);
+                x4[u] = in ? a.ux_in[g] : T(0);
+                z4[u] = in ? a.uz_in[g] : T(0);
+                d4[u] = in ? a.id_in[g] : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int i = i0 + u * nt + tid;
+                if (i < cnt) {
+                    const int d = o0 + i;
+                    pcell[d] = c4[u]; pfrac[d] = f4[u]; pux[d] = x4[u]; puz[d] = z4[u]; pid[d] = d4[u];
+                }
+            }
         }
     }
     const Scal<T> sc = scal_block<T>(I);
@@ -242,6 +268,15 @@ __global__ void __launch_bounds__(PASS_THREADS, 2) pic_pass_kernel(PassArgs<T> a
             s_src[0] = src_e_at<T>(I, a.f.src, t);
             s_src[1] = src_h_at<T>(I, a.f.src, t);
         }
+        // the exact zone at the start of this step: the loaded range less 3 cells a step at each
+        // end that is not a grid end (nothing is missing beyond a grid end); work outside it
+        // cannot reach the own cells, so it is skipped
+        int zlo[2], zhi[2];
+#pragma unroll
+        for (int r = 0; r < NR; ++r) {
+            zlo[r] = llo[r] == 0 ? 0 : llo[r] + 3 * st;
+            zhi[r] = lhi[r] == n ? n : lhi[r] - 3 * st;
+        }
         // ---------------- push ----------------
         for (int i = tid; i < np; i += nt) {
             const int c = pcell[i];
@@ -249,11 +284,11 @@ __global__ void __launch_bounds__(PASS_THREADS, 2) pic_pass_kernel(PassArgs<T> a
             // the region holding c (selected, not indexed: a dynamic index into the per-region
             // arrays would go through local memory)
             const bool r1 = NR == 2 && c >= llo[NR - 1];
-            const int rlo = r1 ? llo[NR - 1] : llo[0], rhi = r1 ? lhi[NR - 1] : lhi[0];
+            const int rlo = r1 ? zlo[NR - 1] : zlo[0], rhi = r1 ? zhi[NR - 1] : zhi[0];
             const int rb = r1 ? base[NR - 1] : base[0];
             // gathers read c-1 .. c+2 and deposits touch c-1 .. c+2: a particle whose cells are
-            // not all loaded is outside the exact zone and is dropped (so are particles that
-            // wrapped out of this CTA's ranges)
+            // not all in the exact zone is dropped (it can no longer reach an own cell; so are
+            // particles that wrapped out of this CTA's ranges)
             if (c - 1 < rlo || c + 2 >= rhi) {
                 pcell[i] = -1;
                 continue;
@@ -308,16 +343,30 @@ __global__ void __launch_bounds__(PASS_THREADS, 2) pic_pass_kernel(PassArgs<T> a
         // ---------------- E phase: Hyp <- Hy, currents out of the words (cleared), e_cell ----
 #pragma unroll
         for (int r = 0; r < NR; ++r) {
-            for (int k = llo[r] + tid; k < lhi[r]; k += nt) {
+            for (int k = zlo[r] + tid; k < zhi[r]; k += nt) {
                 const int l = k - base[r];
                 hyp[l] = hy[l];
                 const T jxk = Fix<T>::join2(jw, (size_t)LL, l, a.jinv, a.jinv_f);
 #pragma unroll
                 for (int w = 0; w < W; ++w) jw[(size_t)w * LL + l] = 0ull;
                 const bool own = k >= olo[r] && k < ohi[r];
-                if (k >= 1 && k > llo[r])  // Ex over [1, nz]; cell k reads Hy[k-1]
-                    e_cell<T>(I, sc, kr, s, k, src_e, src_h, true, jxk,
-                              (last && own) ? a.gA : nullptr, &nfb, true);
+                if (k >= 1 && k > zlo[r]) {  // Ex over [1, nz]; cell k reads Hy[k-1]
+                    // interior cells take e_cell's operations without its terms that vanish
+                    // there (the streaming E kernel's forms: the same bits)
+                    const int kd = cell_kind(I, k);
+                    if (kd == CELL_VACUUM) {
+                        ex[l] = ex[l] + mul_c((hy[l] - hy[l - 1]) - jxk, sc.ue, sc.ue_lo);
+                    } else if (kd == CELL_KERR) {
+                        const T d = dx[l] + mul_c((hy[l] - hy[l - 1]) - jxk, sc.dtdz, sc.dtdz_lo);
+                        const T A = kr.root(d, sc.eps0, &nfb);
+                        if (last && own) a.gA[k] = A;
+                        dx[l] = d;
+                        ex[l] = div_c(d, sc.e0r + sc.e0chi * A, sc.e0r_rel);
+                    } else {
+                        e_cell<T>(I, sc, kr, s, k, src_e, src_h, true, jxk,
+                                  (last && own) ? a.gA : nullptr, &nfb, true);
+                    }
+                }
                 if (last && own) {
                     a.jx_out[k] = jxk;
                     a.jz_out[k] = Fix<T>::join2(jw + (size_t)W * LL, (size_t)LL, l, a.jinv, a.jinv_f);
@@ -328,8 +377,14 @@ __global__ void __launch_bounds__(PASS_THREADS, 2) pic_pass_kernel(PassArgs<T> a
         // ---------------- H phase ----------------
 #pragma unroll
         for (int r = 0; r < NR; ++r) {
-            const int khi = min(lhi[r] - 1, n - 1);  // Hy over [1, nz-1]; cell k reads Ex[k+1]
-            for (int k = max(llo[r], 1) + tid; k < khi; k += nt) h_cell<T>(I, sc, s, k, src_h);
+            const int khi = min(zhi[r] - 1, n - 1);  // Hy over [1, nz-1]; cell k reads Ex[k+1]
+            for (int k = max(zlo[r], 1) + tid; k < khi; k += nt) {
+                const int l = k - base[r];
+                if (cell_kind(I, k) != CELL_GENERIC)  // interior: h_cell with den = 1
+                    hy[l] = hy[l] + mul_c(ex[l + 1] - ex[l], sc.uh, sc.uh_lo);
+                else
+                    h_cell<T>(I, sc, s, k, src_h);
+            }
         }
         if (tid == 0) {
             const int jt = I.nzsrc - 1;
@@ -369,8 +424,8 @@ __global__ void __launch_bounds__(PASS_THREADS, 2) pic_pass_kernel(PassArgs<T> a
                 go[(int64_t)FDTD_ST_P * n + k] = pc[l];
                 go[(int64_t)FDTD_ST_PPREV * n + k] = pp[l];
             }
-            if (u.psie) go[(int64_t)FDTD_ST_PSIE * n + k] = psie[l];
-            if (u.psih) go[(int64_t)FDTD_ST_PSIH * n + k] = psih[l];
+            if (u.psie) go[(int64_t)FDTD_ST_PSIE * n + k] = psie[pml_col(I, k)];
+            if (u.psih) go[(int64_t)FDTD_ST_PSIH * n + k] = psih[pml_col(I, k)];
         }
     }
     // ---- write back: particles whose cell lies in an own range, by group; one shared atomic
@@ -537,9 +592,12 @@ inline PassGeom pass_geometry(int tsize, const FdtdInstance &h, const PicBeam &b
     g.capE = ((int)(2.0 * ppc * g.H) + 256 + 3) & ~3;
     g.capM = ((int)(2.0 * ppc * g.wmax) + 512 + 3) & ~3;
     g.stride = 2 * g.capE + g.capM;
-    g.pcap = ((int)(1.5 * ppc * g.Lmax) + 512 + 3) & ~3;
-    g.smem1 = pass_smem_bytes(tsize, 1, g.Lmax, g.pcap);
-    g.smem2 = pass_smem_bytes(tsize, 2, g.Lmax, g.pcap);
+    // a loaded range holds ~ppc Lmax particles; a quarter more and 256 cover the fluctuations
+    // of a beam of even density (a shortfall is reported, FDTD_STATUS_OVERFLOW)
+    g.pcap = ((int)(1.25 * ppc * g.Lmax) + 256 + 3) & ~3;
+    const int lin = h.mode == FDTD_MODE_LINLOR ? 1 : 0;
+    g.smem1 = pass_smem_bytes(tsize, 1, g.Lmax, g.pcap, lin, 2 * h.pml + 1);
+    g.smem2 = pass_smem_bytes(tsize, 2, g.Lmax, g.pcap, lin, 2 * h.pml + 1);
     // 1 KiB stays for the kernel's static shared variables
     g.ok = g.smem2 <= smem_optin - 1024;
     return g;
