@@ -407,7 +407,7 @@ def bench_sweep(args, flush):
             "plain_mcell_steps_per_s": round(plain_rate / 1e6, 1),
             "plain_global_mcell_steps_per_s": round(global_rate / 1e6, 1),
             "vs_plain": round(batched / best_plain, 1),
-            "dft": "tcgen05 split-BF16x3, FP32 chunk sums, FP64 across chunks",
+            "dft": "tcgen05 split-BF16x3, FP32 sums over 1024-step groups, compensated FP32 sums across groups",
             "dft_gemm_tflops": round(dft_flops / (spectra_ms * 1e-3) / 1e12, 2),
             "dft_tensor_tflops": round(3 * dft_flops / (spectra_ms * 1e-3) / 1e12, 2),
             "dft_cuda_core_ms": round(min(c_ms), 2), "dft_tc_error": sw.dft_error(),
