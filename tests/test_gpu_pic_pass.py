@@ -99,3 +99,30 @@ def test_pass_path_refuses_what_it_cannot_run():
                  pass_steps=32, tile_cells=128)  # halo 100 cells > half a 128-cell tile
     with pytest.raises(FdtdPicError):
         run.step(10)
+
+
+def test_pass_path_long_grid_equals_streaming():
+    """2^21 cells and 2^23 particles (4 a cell, the large instance's density; 513-cell tiles
+    with an odd number of loaded cells): the pass path gives the streaming kernels' bits through
+    a call's last step (Jz deposited too)."""
+    torch = _torch()
+    import scipy.constants as sc
+    from fdtdpic.grid import lorentz_kerr_grid
+    from fdtdpic.pic import PicRun, make_beam
+    nz, steps, npart = 1 << 21, 64, 1 << 23
+    out = []
+    for path in ("streaming", "pass"):
+        g = lorentz_kerr_grid(nz, steps, front=nz // 4, rear=3 * nz // 4, nzsrc=100,
+                              probes=(50, nz - 50), chi3=1e-2)
+        beam = make_beam(npart, 50, nz - 51, DZ, seed=11, sort=False)
+        beam.ux[:] = 0.01  # transverse momentum from the start: every step deposits Jx
+        run = PicRun(g, beam, DZ, DT, sc.mu_0, precision="f32", path=path)
+        run.step(steps)
+        torch.cuda.synchronize()
+        jx, jz = run.currents()
+        out.append(dict(state=run.d_state.cpu().numpy(), hyp=run.d_hyp.cpu().numpy(), jx=jx,
+                        jz=jz, probes=run.probes(), parts=run.particles(), status=run.status()))
+        del run
+    want, got = out
+    assert np.abs(want["jx"]).max() > 0
+    _equal(got, want)
