@@ -39,6 +39,9 @@ UNIT = "Mcell-steps/s + Mparticle-steps/s"
 WORKLOAD = "fdtd_pic_1inst_nz4096_steps8192_np1048576"
 BYTES_PER_PARTICLE = 24  # z, ux, uz read + write at 4 B (6p, p = 4)
 BYTES_PER_CELL = 16      # Ex, Hy read + write at 4 B (4p)
+# particles re-binned by cell every SORT_EVERY steps (64 measured best on GB300 for the headline:
+# 114.8 ms a run against 117.4 at 32, 123.1 at 16; the results are the same bits at any interval)
+SORT_EVERY = 64
 
 
 def _peaks():
@@ -126,7 +129,7 @@ def _setup(precision):
     grid = lorentz_kerr_grid(NZ, T, front=FRONT, rear=REAR, nzsrc=NZSRC, probes=PROBES, chi3=1e-2)
     beam = make_beam(NP, CLO, CHI, DZ)
     dt = 0.5 * DZ / 299792458.0
-    run = PicRun(grid, beam, DZ, dt, sc.mu_0, precision=precision, sort_every=32)
+    run = PicRun(grid, beam, DZ, dt, sc.mu_0, precision=precision, sort_every=SORT_EVERY)
     return grid, beam, run, dt
 
 
@@ -264,10 +267,10 @@ def _headline(args, precision, steps, warmup, flush, world, local):
             pass
     # our kernels per run (the beam lies inside its domain, so each push launch carries the
     # previous step's H phase): push and E phase per step, a standalone H phase before each
-    # re-binning and at each block's end (every 32 steps), five re-binning kernels (histogram,
-    # three-launch scan, scatter) every 32 steps, the step counter's advance per 64-step graph
-    # block, and init, constants, step-counter set and finish per run
-    launches_per_run = 2 * T + 6 * (T // 32) + T // 64 + 4
+    # re-binning and at each block's end (one per SORT_EVERY steps), five re-binning kernels
+    # (histogram, three-launch scan, scatter) every SORT_EVERY steps, the step counter's advance
+    # per graph block (2 SORT_EVERY steps), and init, constants, step-counter set and finish
+    launches_per_run = 2 * T + 6 * (T // SORT_EVERY) + T // (2 * SORT_EVERY) + 4
     return dict(ms=ms, value=units * world / (ms * 1e-3) / 1e6, clocks=clk.summary(),
                 e2e={"value": round(units * world / (e2e_ms * 1e-3) / 1e6, 1), "unit": UNIT,
                      "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -307,7 +310,7 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if args.precision == "f32" else "f64", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "nz": NZ, "time_steps": T, "n_part": NP,
-                   "slab": [FRONT, REAR], "mode": "kerr", "sort_every": 32,
+                   "slab": [FRONT, REAR], "mode": "kerr", "sort_every": SORT_EVERY,
                    "l2": "flushed between timed steps (256 MiB write)",
                    "parallelism": f"one instance per GPU x{world}"},
         "mcell_steps_per_s": round(NZ * T * world / (ms * 1e-3) / 1e6, 1),

@@ -1233,9 +1233,14 @@ int launch_pic(int precision_bytes, const FdtdInstance &h, const BatchArgs<T> &f
         P.fuse_h = !P.fused && bm.n_part > 0 && inside && slots > 0 &&
                    (bm.path & FDTDPIC_PATH_CELLS_INSIDE) && (long long)P.pblocks <= 4 * slots;
         // a latency-bound step runs faster with fewer particles per thread (768 a CTA measured
-        // best on GB300 for a one-to-two-wave beam; 1024 for many waves)
+        // best on GB300 for a one-to-two-wave beam); a launch of more than four waves with more
+        // (on the 64M-particle instance, ms a step: 4096 a CTA 0.675, 2048 0.687, 1024 0.729,
+        // 512 0.830)
         if (P.fuse_h && bm.chunk == 0) {
             pa.chunk = 768;
+            P.pblocks = (bm.n_part + pa.chunk - 1) / pa.chunk;
+        } else if (bm.chunk == 0 && slots > 0 && (long long)P.pblocks > 4 * slots) {
+            pa.chunk = 4096;
             P.pblocks = (bm.n_part + pa.chunk - 1) / pa.chunk;
         }
     }
