@@ -68,3 +68,15 @@ def compat_objects(g):
     C_P.kappaMax, C_P.alphaMax = float(g["kappaMax"]), float(g["alphaMax"])
     C_V = MC.CPML_Variables(P.Nz, P.timeSteps)
     return V, P, C_V, C_P
+
+
+def acubic_bound(want, kerr, dx_rel=1e-10):
+    """Per-cell bound on the Kerr amplitude A of a whole run against the reference's.  The
+    reference's closed form returns x = 2 j cos(k/3) - b/3a with b/3a far larger than the root,
+    so last-place differences between two libraries' pow/acos/cos reach the root magnified by
+    |b/3a| / |x|: 64 units in the last place of |b/3a|.  The root also carries the run's own
+    difference in Dx (d = -(Dx/eps0)^2 feeds it with twice Dx's relative error, and
+    x ~ -d / c): dx_rel of |x|."""
+    a, b = float(kerr[0]), float(kerr[1])
+    shift = abs(b / (3.0 * a)) if a != 0.0 else 0.0
+    return 64.0 * np.finfo(float).eps * shift + dx_rel * np.abs(want)

@@ -3,7 +3,7 @@
 import numpy as np
 import pytest
 
-from helpers import RUN_CASES, compat_objects, integrator_of, load
+from helpers import RUN_CASES, acubic_bound, compat_objects, integrator_of, load
 
 from oracle import oracle as O
 
@@ -40,7 +40,10 @@ def test_controller_matches_reference(name, monkeypatch):
         assert O.rel_l2(got, g[key]) <= F64_TOL, key
     assert O.rel_l2(V.Dx, g["Dx"]) <= 1e-11
     if integrator_of(g) == "IntegratorNL1D":
-        assert O.rel_l2(V.Acubic, g["Acubic"]) <= 1e-6
+        # per cell: the closed form's conditioning and the run's Dx difference (helpers)
+        from fdtdpic import physics_setup as ps
+        bound = acubic_bound(g["Acubic"], ps.kerr_coefficients(P, V, V.plasmaFreqE))
+        assert np.all(np.abs(np.asarray(V.Acubic) - g["Acubic"]) <= bound)
     if "Ex_History" in g.files:
         assert V.Ex_History.shape == g["Ex_History"].shape
         assert O.rel_l2(V.Ex_History, g["Ex_History"]) <= F64_TOL

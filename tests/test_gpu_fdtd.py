@@ -3,7 +3,7 @@
 import numpy as np
 import pytest
 
-from helpers import RUN_CASES, integrator_of, load, ref_objects, sources_of
+from helpers import RUN_CASES, acubic_bound, integrator_of, load, ref_objects, sources_of
 
 from oracle import oracle as O
 
@@ -48,7 +48,9 @@ def _compare(g, grids, res, tol):
     if integ == "IntegratorNL1D":
         assert O.rel_l2(last.probes[:, 0], g["Port1"]) <= tol
         assert O.rel_l2(last.probes[:, 1], g["Port2"]) <= tol
-        assert O.rel_l2(last.Acubic, g["Acubic"]) <= 1e-6
+        # per cell: the closed form's conditioning and the run's Dx difference (helpers)
+        bound = acubic_bound(g["Acubic"], grids[-1].kerr)
+        assert np.all(np.abs(last.Acubic - g["Acubic"]) <= bound)
     elif integ == "IntegratorLinLor1D":
         assert O.rel_l2(res[0].probes[:, 0], g["x1ColBe"]) <= tol
         assert O.rel_l2(res[1].probes[:, 1], g["x1ColAf"]) <= tol
