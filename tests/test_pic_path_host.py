@@ -1,7 +1,8 @@
 """Host side of the beam step's path selection (no GPU): PicRun sets FDTDPIC_PATH_CELLS_INSIDE
 exactly when every cell of its host beam lies in [clo, chi), and fdtdpic_run refuses path words
-with unknown bits or an unknown path before any device work (its device pointers here are
-placeholders that a refused call never reads)."""
+with unknown bits or an unknown path, and temporally blocked passes (mode 3) whose tiling does not
+apply, before any device work (its device pointers here are placeholders that a refused call never
+reads)."""
 import ctypes
 from types import SimpleNamespace
 
@@ -42,6 +43,8 @@ def test_run_refuses_unknown_path_bits():
                              ctypes.byref(pb), None, None, None, None, None, fake, fake, fake,
                              fake, scratch_bytes, fake, None, None)
 
+    # 32, 15, -1: bits outside the mode and the CELLS_INSIDE flag; 3: passes without the flag;
+    # 16 | 3: passes over an empty beam, which have no tiling
     for path in (32, 3, 15, 16 | 3, -1):
         assert run(path, 0) == -1, path  # FDTDPIC_ERR_ARG
     # accepted path words get past that check to the scratch-size check (FDTDPIC_ERR_OOM),
