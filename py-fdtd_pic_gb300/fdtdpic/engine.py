@@ -94,7 +94,10 @@ def upload(grids, precision="f64", device=None) -> Packed:
 
 
 def launch(p: Packed, stream=None, threads=256, grid_ctas=0):
-    """Enqueue every grid of the batch on ``stream`` (default: torch's current stream)."""
+    """Enqueue every grid of the batch on ``stream`` (default: torch's current stream).
+    :func:`upload` queues its copies and zero fills on the stream that was current then; a
+    caller launching on another stream first makes it wait for that one
+    (``stream.wait_stream(torch.cuda.current_stream())``)."""
     L = lib()
     st = ctypes.c_void_p((stream or torch.cuda.current_stream()).cuda_stream)
     if p.resident:

@@ -161,16 +161,22 @@ class PicRun:
         self.pb.path = self.path_mode | (PATH_CELLS_INSIDE if inside else 0)
 
     def step(self, n_steps, stream=None, timing=None):
-        """Enqueue the next n_steps steps (asynchronous unless ``timing`` is given: then the
-        call runs launch by launch and fills the FdtdPicTiming with per-kernel GPU time)."""
+        """Enqueue the next n_steps steps on ``stream`` (default: torch's current stream; the
+        run's buffers are set up on the stream current at construction, which another stream
+        first waits for).  Asynchronous unless ``timing`` is given: then the call runs launch
+        by launch and fills the FdtdPicTiming with per-kernel GPU time."""
         g = self.grid
         t0 = self.step_done
         t1 = min(g.n_steps, t0 + n_steps)
         d = self.desc.copy()
         d["step_begin"], d["step_end"] = t0, t1
         d["resume"] = 1 if t0 > 0 else 0
-        self.d_desc.copy_(torch.from_numpy(d.view(np.uint8).copy()).to(self.dev), non_blocking=False)
-        st = ctypes.c_void_p((stream or torch.cuda.current_stream()).cuda_stream)
+        s = stream or torch.cuda.current_stream(self.dev)
+        # the descriptor goes in on the launch stream: after the work already queued there (which
+        # reads the previous call's descriptor), before this call's kernels
+        with torch.cuda.stream(s):
+            self.d_desc.copy_(torch.from_numpy(d.view(np.uint8).copy()), non_blocking=False)
+        st = ctypes.c_void_p(s.cuda_stream)
         check(self.L.fdtdpic_run(
             self.prec, d.ctypes.data, _ptr(self.d_desc), _ptr(self.d_table), _ptr(self.d_src),
             _ptr(self.d_state), _ptr(self.d_probe), ctypes.byref(self.pb), _ptr(self.d_cell),

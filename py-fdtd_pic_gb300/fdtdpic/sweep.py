@@ -190,6 +190,8 @@ class Sweep:
         return g
 
     def run(self, stream=None):
+        """Replay the captured graph, or enqueue the sequence on ``stream`` (default: torch's
+        current stream; another stream first waits for the stream the batch was uploaded on)."""
         if self.graph is not None:
             self.graph.replay()
         else:

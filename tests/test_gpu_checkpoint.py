@@ -65,6 +65,28 @@ def test_snapshot_restore_equals_uninterrupted_run(precision, case):
     assert snap.nbytes() > 0
 
 
+@pytest.mark.parametrize("case", ["nz512", "nz1536_fused"])
+def test_calls_on_a_side_stream_equal_one_call(case):
+    """step(n, stream=s) calls queued back to back on a stream other than the current one, with
+    no host wait between them: each call's descriptor (its step range) goes in on s, behind the
+    previous call's kernels, so the run equals one call on the current stream bit for bit."""
+    torch, whole = _run("f32", case)
+    whole.step(T)
+    want = _all(whole)
+    del whole
+    _, run = _run("f32", case)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())  # the run's buffers were set up on this one
+    for n in (100, 37, 200, 263):
+        run.step(n, stream=s)
+    assert run.step_done == T
+    got = _all(run)
+    for k in ("state", "hyp", "jx", "jz", "probes"):
+        np.testing.assert_array_equal(got[k], want[k], err_msg=k)
+    for a, b in zip(got["parts"], want["parts"]):
+        np.testing.assert_array_equal(a, b)
+
+
 def test_restore_refuses_another_shape():
     torch, a = _run("f32", "nz512")
     _, b = _run("f64", "nz512")
