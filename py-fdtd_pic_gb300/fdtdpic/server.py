@@ -216,7 +216,10 @@ class Server:
         self._ready: collections.deque = collections.deque()
         self._ready_cv = threading.Condition()
         self._prefetch = max(1, int(prefetch))
+        # submitted and not yet admitted: submit() may run on another thread than the
+        # scheduling one, so the count changes under a lock
         self._unadmitted = 0
+        self._count_lock = threading.Lock()
         self._closing = False
         # requests for the streaming kernels are recognised on submission and prepared by a
         # second thread, at most max_big ahead, so they never hold up the rounds' requests
@@ -267,8 +270,13 @@ class Server:
         """Requests submitted and not yet admitted."""
         return self._unadmitted
 
+    def _count(self, d: int):
+        with self._count_lock:
+            self._unadmitted += d
+
     def submit(self, req: Request):
-        self._unadmitted += 1
+        """Queue a request (any thread)."""
+        self._count(1)
         self._inbox.put(req)
 
     def cancel(self, rid: int):
@@ -404,7 +412,7 @@ class Server:
     def _admit_one(self, req: Request, need: int, now: float, big: bool) -> bool:
         """Place one request taken off a ready queue.  False when its allocation failed while
         other requests hold memory: it goes back to the head of its queue to wait for them."""
-        self._unadmitted -= 1
+        self._count(-1)
         if req._error is not None:
             self._fail(req, now, f"prepare: {type(req._error).__name__}: {req._error}")
             return True
@@ -423,7 +431,7 @@ class Server:
         except (torch.cuda.OutOfMemoryError, MemoryError) as e:
             if self.active or self.big or self.inflight:
                 self.oom_retries += 1
-                self._unadmitted += 1
+                self._count(1)
                 with self._ready_cv:
                     (self._big_ready if big else self._ready).appendleft(req)
                 return False
