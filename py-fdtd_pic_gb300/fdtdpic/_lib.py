@@ -5,6 +5,7 @@ There is no CPU fallback: if the library is missing or cannot be loaded, :func:`
 from __future__ import annotations
 
 import ctypes
+import fcntl
 import os
 import subprocess
 import threading
@@ -62,14 +63,25 @@ def _stale() -> bool:
     t = os.path.getmtime(LIB_PATH)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     deps += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+    deps.append(os.path.abspath(__file__))  # the units' nvcc flags
     return any(os.path.getmtime(d) > t for d in deps)
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile every translation unit for sm_103a (in parallel) and link libfdtdpic.so."""
+    """Compile every translation unit for sm_103a (in parallel) and link libfdtdpic.so.
+    Processes building at once take turns (a lock file in the build folder): the object files
+    have fixed names."""
     if not force and not _stale():
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
+    with open(os.path.join(BUILD_DIR, ".lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        if not force and not _stale():  # another process built it meanwhile
+            return LIB_PATH
+        return _build_locked(verbose)
+
+
+def _build_locked(verbose: bool) -> str:
     nvcc = _nvcc()
     common = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "-I", INCLUDE, "-I", CSRC]
