@@ -226,10 +226,13 @@ typedef struct PicBeam {
                            2: persistent tiled kernel, 3: temporally blocked passes (long
                            grids: sort_every whole steps per launch, 0 for 8, over tiles of
                            about chunk cells, 0 for 512, each tile's fields and particles in
-                           shared memory; needs FDTDPIC_PATH_CELLS_INSIDE, else
-                           FDTDPIC_ERR_ARG, as for tiles narrower than twice the pass's halo
-                           of 3 sort_every + 4 cells); may be or-ed with
-                           FDTDPIC_PATH_CELLS_INSIDE */
+                           shared memory; FDTDPIC_ERR_ARG without
+                           FDTDPIC_PATH_CELLS_INSIDE, for an empty beam, fewer than five
+                           tiles, tiles narrower than twice the pass's halo H = 3 sort_every
+                           + 4 cells, clo or chi within H cells of an edge of its tile (the
+                           grid's ends excepted), the two tiles holding clo and chi within 2H
+                           cells of each other, or a tile beyond shared memory); may be or-ed
+                           with FDTDPIC_PATH_CELLS_INSIDE */
     double kE;     /* q dt / (2 m c) */
     double kH;     /* -q mu0 dt / (2 m) */
     double sc;     /* c dt / dz */
@@ -288,7 +291,7 @@ int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d
  * that overlap on the GPU race: serialise them.  The first call on a device looks up the array's
  * address (make it before any stream capture) and keeps it for the device's context: do not call
  * this entry point on a device after cudaDeviceReset.  Streaming kernels only: beam->path takes
- * the bits fdtdpic_run takes with mode 0 or 1 (mode 2, the tiled path, returns
+ * the bits fdtdpic_run takes with mode 0 or 1 (modes 2 and 3, the tiled and pass paths, return
  * FDTDPIC_ERR_ARG).  Launches kernel by kernel; no cudaMalloc, no graph capture, no event or
  * stream creation. */
 int fdtdpic_run_noalloc(int precision, const FdtdInstance *h_inst, const FdtdInstance *d_inst,
