@@ -75,7 +75,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
     with open(os.path.join(BUILD_DIR, ".lock"), "w") as lock:
-        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            fcntl.flock(lock, fcntl.LOCK_EX)
+        except OSError:  # a file system without locks: build unlocked, as a single process
+            pass
         if not force and not _stale():  # another process built it meanwhile
             return LIB_PATH
         return _build_locked(verbose)
