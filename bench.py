@@ -256,9 +256,11 @@ def _headline(args, precision, steps, warmup, flush, world, local):
         achieved = bpp * NP / (per_launch * 1e-3) / 1e9
         roof.update(achieved=round(achieved, 1), frac=round(achieved / peak, 3))
         l2 = l2_copy_gbs(dev)
+        beam_mib = NP * (4 + 3 * (8 if precision == "f64" else 4)) / 2 ** 20
         roof.update(l2_gbs=round(l2, 1), l2_frac=round(achieved / l2, 3),
-                    l2_note="the beam (16 MiB in FP32) and fields stay in L2 between steps: "
-                            "l2_frac is achieved / a live L2-resident copy's bandwidth")
+                    l2_note="the beam (%d MiB: cell, frac, ux, uz) and fields stay in L2 "
+                            "between steps: l2_frac is achieved / a live L2-resident copy's "
+                            "bandwidth" % beam_mib)
     prof = os.path.join(ROOT, "profiles", "pic_push_kernel_traffic.json")
     if os.path.exists(prof) and precision == "f32":
         try:
@@ -507,16 +509,37 @@ def bench_large(args, flush):
     alg = (nz * BYTES_PER_CELL + slab * 8 + nz * 8 + npart * BYTES_PER_PARTICLE)
     peak, kind = _peaks()
     gbs = alg * n / (ms * 1e-3) / 1e9
-    return {"workload": "large_nz16777216_np67108864_kerr_f32", "timed_steps": n,
-            "ms_per_step": round(ms / n, 3),
-            "mcell_steps_per_s": round(nz * n / (ms * 1e-3) / 1e6, 1),
-            "mparticle_steps_per_s": round(npart * n / (ms * 1e-3) / 1e6, 1),
-            "algorithmic_gbs": round(gbs, 1), "hbm_frac": round(gbs / peak, 3),
-            "peak_source": kind, "bytes_per_step": alg,
-            "kernel_ms_per_step": {"push": round(tm.push_ms / 64, 3),
-                                   "field": round(tm.field_ms / 64, 3),
-                                   "sort": round(tm.sort_ms / 64, 3)},
-            "status": [int(x) for x in run.status()]}
+    out = {"workload": "large_nz16777216_np67108864_kerr_f32", "timed_steps": n,
+           "ms_per_step": round(ms / n, 3),
+           "mcell_steps_per_s": round(nz * n / (ms * 1e-3) / 1e6, 1),
+           "mparticle_steps_per_s": round(npart * n / (ms * 1e-3) / 1e6, 1),
+           "algorithmic_gbs": round(gbs, 1), "hbm_frac": round(gbs / peak, 3),
+           "peak_source": kind, "bytes_per_step": alg,
+           "kernel_ms_per_step": {"push": round(tm.push_ms / 64, 3),
+                                  "field": round(tm.field_ms / 64, 3),
+                                  "sort": round(tm.sort_ms / 64, 3)},
+           "status": [int(x) for x in run.status()]}
+    # beside the algorithmic count: the DRAM traffic ncu measured for a step's launches
+    dram = _large_dram_bytes_per_step()
+    if dram:
+        dgbs = dram * n / (ms * 1e-3) / 1e9
+        out.update(dram_bytes_per_step=int(dram), dram_gbs=round(dgbs, 1),
+                   dram_frac=round(dgbs / peak, 3),
+                   dram_source="ncu DRAM bytes of a step's push, E and H launches "
+                               "(profiles/pic_kernels_large_half.json: half size x 2; the "
+                               "re-binning launches not included) / this run's ms_per_step")
+    return out
+
+
+def _large_dram_bytes_per_step():
+    """DRAM bytes of one full-size large-instance step (its push, E and H launches), from the
+    committed ncu capture of the same kernels at half size, or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "pic_kernels_large_half.json")) as f:
+            d = json.load(f)
+        return float(d["half_size_dram_bytes_per_step"]) * float(d["scale_to_full_size"])
+    except Exception:
+        return None
 
 
 def bench_variants(args, flush):
