@@ -154,7 +154,6 @@ __global__ void __launch_bounds__(TILE_THREADS, 1) pic_tiled_kernel(TileArgs<T> 
     const int n = I.nz + 1;
     const int c0 = tile_begin(b, a.G, n);
     const int c1 = tile_begin(b + 1, a.G, n);
-    const int wt = c1 - c0;
     const int base = c0 - 1;
     const int L = a.w + 3;  // local nodes base .. base+L-1 = c0-1 .. c1+1 (max width)
 
