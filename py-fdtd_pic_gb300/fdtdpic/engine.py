@@ -15,8 +15,8 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import F32, F64, INSTANCE_DTYPE, ST, STATE_ARRAYS, check, lib
-from .grid import Grid, pack
+from ._lib import F32, F64, INSTANCE_DTYPE, ST, check, lib
+from .grid import pack
 
 
 def _require_cuda():

@@ -12,7 +12,7 @@ from dataclasses import dataclass
 import numpy as np
 import torch
 
-from ._lib import F32, F64, INSTANCE_DTYPE, ST, STATE_ARRAYS, check, lib
+from ._lib import F64, ST, check, lib
 from .engine import _dtype, _ptr, _require_cuda
 from .grid import Grid, pack
 

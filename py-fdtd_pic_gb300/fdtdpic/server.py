@@ -36,7 +36,7 @@ import numpy as np
 import torch
 
 from . import physics_setup as ps
-from ._lib import F32, F64, INSTANCE_DTYPE, STATE_ARRAYS, check, lib
+from ._lib import F64, INSTANCE_DTYPE, STATE_ARRAYS, check, lib
 from .engine import _dtype, _require_cuda
 from .grid import Grid, lorentz_kerr_grid, pack
 from .pic import C0, Beam, PicBeam, PicRun, beam_constants

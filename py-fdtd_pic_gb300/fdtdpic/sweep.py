@@ -19,7 +19,6 @@ from __future__ import annotations
 import ctypes
 import json
 import os
-import time
 from dataclasses import dataclass
 
 import numpy as np
@@ -27,7 +26,7 @@ import torch
 
 from . import engine
 from . import physics_setup as ps
-from ._lib import F32, F64, MODE_KERR, check, lib
+from ._lib import MODE_KERR, check, lib
 from .grid import lorentz_kerr_grid
 
 DZ = 0.015

@@ -1,7 +1,5 @@
 """The beam model's own checks, on the CPU oracle (no GPU): analytic Boris orbits and exact
 discrete charge conservation of the Jz deposit."""
-import ctypes
-
 import numpy as np
 
 from oracle import oracle as O
