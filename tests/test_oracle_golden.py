@@ -86,6 +86,17 @@ def test_named_cubic_answers():
     assert abs(O.cubic_solve(4.9e-7, 2e-3, 4, -1)[0] - 0.249968756) < 1e-9
 
 
+def test_benchmark_cubic_of_the_reference():
+    """The Kerr-type cubic the reference times in benchmarkTests.py (-81 x^3 + 4 x^2 + 2e-5 x +
+    2e-16, solved there with np.roots, taking the first real root >= 0): roots[0] of the
+    restated closed form is that root."""
+    co = (-81.0, 4.0, 2e-5, 2e-16)
+    want = next(x for x in np.roots(co) if x >= 0 and np.imag(x) == 0).real
+    for got in (complex(O.cubic_solve(*co)[0]), complex(O.cubic_solve_py(*co)[0])):
+        assert got.imag == 0.0
+        assert abs(got.real - want) <= 1e-15 * want, (got, want)
+
+
 def test_env_and_mat_setup_match_reference():
     g = np.load(os.path.join(GOLDEN, "setup.npz"))
     for args, want in zip(g["env_in"], g["env_out"]):
