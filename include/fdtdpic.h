@@ -50,6 +50,13 @@ typedef struct CUstream_st *fdtdpic_stream_t; /* == cudaStream_t */
 #define FDTDPIC_F64 8 /* precision argument: FP64 state (parity path) */
 #define FDTDPIC_F32 4 /* FP32 state, FP64 near-degenerate cubic solves */
 
+/* Size limits: the kernels index cells and particles with 32-bit integers, with headroom for
+ * per-launch offsets.  Every entry point refuses a larger FdtdInstance.nz, and fdtdpic_run and
+ * fdtdpic_slot_check a larger beam, with FDTDPIC_ERR_ARG before any device work
+ * (fdtdpic_run_noalloc's 24 MiB scratch refuses such a beam first, with FDTDPIC_ERR_OOM). */
+#define FDTDPIC_MAX_CELLS (1 << 30)     /* FdtdInstance.nz */
+#define FDTDPIC_MAX_PARTICLES (1 << 30) /* PicBeam.n_part, FdtdSlot.n_part */
+
 /* Per-instance status bits (d_status[i]) */
 #define FDTD_STATUS_NONFINITE 1 /* Ex or Hy not finite at the end of the call */
 #define FDTD_STATUS_SKIPPED 2   /* instance larger than smem_bytes: not run */

@@ -126,7 +126,8 @@ cudaStream_t pic_capture_stream()
 
 int check_instance(const FdtdInstance &I)
 {
-    if (I.nz < 2 || I.n_steps < 0 || I.step_begin < 0 || I.step_end < I.step_begin ||
+    if (I.nz < 2 || I.nz > FDTDPIC_MAX_CELLS || I.n_steps < 0 || I.step_begin < 0 ||
+        I.step_end < I.step_begin ||
         I.step_end > I.n_steps)
         return FDTDPIC_ERR_ARG;
     if (I.pml < 0 || 2 * (int64_t)I.pml + 1 > (int64_t)I.nz + 1) return FDTDPIC_ERR_ARG;
@@ -312,8 +313,9 @@ int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d
     if (rc != FDTDPIC_OK) return rc;
     const PicBeam &b = *beam;
     // |cell displacement| per step < sc must stay below one cell for the Jz deposit
-    if (b.n_part < 0 || b.clo < 2 || b.chi <= b.clo || b.chi > h_inst->nz - 2 || b.sort_every < 0 ||
-        b.chunk < 0 || !(b.jscale > 0.0) || !(b.sc > 0.0 && b.sc < 1.0))
+    if (b.n_part < 0 || b.n_part > FDTDPIC_MAX_PARTICLES || b.clo < 2 || b.chi <= b.clo ||
+        b.chi > h_inst->nz - 2 || b.sort_every < 0 || b.chunk < 0 || !(b.jscale > 0.0) ||
+        !(b.sc > 0.0 && b.sc < 1.0))
         return FDTDPIC_ERR_ARG;
     if (b.n_part > 0 && (!d_cell || !d_frac || !d_ux || !d_uz || !d_id)) return FDTDPIC_ERR_ARG;
     if (precision != FDTDPIC_F64 && precision != FDTDPIC_F32) return FDTDPIC_ERR_ARG;

@@ -589,6 +589,13 @@ inline PassGeom pass_geometry(int tsize, const FdtdInstance &h, const PicBeam &b
     g.ok = g.wmin >= 2 * g.H && lo_ok && hi_ok && lo1 + g.H <= hi0 - g.H;
     if (!g.ok) return g;
     const double ppc = (double)bm.n_part / (double)(bm.chi - bm.clo);
+    // capacities within the int arithmetic (far beyond what shared memory holds: such a beam
+    // takes another path); H < wmax and Lmax <= 2 wmax, so these two bound all three
+    const double int_room = (double)(1 << 30);
+    if (2.0 * ppc * g.wmax + 1024 > int_room || 1.25 * ppc * g.Lmax + 1024 > int_room) {
+        g.ok = false;
+        return g;
+    }
     g.capE = ((int)(2.0 * ppc * g.H) + 256 + 3) & ~3;
     g.capM = ((int)(2.0 * ppc * g.wmax) + 512 + 3) & ~3;
     g.stride = 2 * g.capE + g.capM;

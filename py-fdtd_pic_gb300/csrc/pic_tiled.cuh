@@ -612,6 +612,12 @@ inline TileGeom tile_geometry(const FdtdInstance &h, const PicBeam &bm, int sms)
     g.wmax = (n + G - 1) / G;
     const int wlo = n / G;
     const double per_cell = (double)bm.n_part / (double)(bm.chi - bm.clo);
+    // segment capacities within the int arithmetic (such a beam takes the streaming path)
+    const double int_room = (double)(1 << 30);
+    if (2.0 * per_cell * g.wmax + 1024 > int_room || 4.0 * per_cell + 256 > int_room) {
+        g.ok = false;
+        return g;
+    }
     g.cap = (int)(2.0 * per_cell * g.wmax) + 1024;
     g.mig_cap = (int)(4.0 * per_cell) + 256;
     g.wrap_lo = tile_of(bm.clo, G, n);

@@ -88,7 +88,7 @@ int fdtdpic_slot_check(int precision, const FdtdSlot *s)
     if (check_instance(I) != FDTDPIC_OK) return FDTDPIC_ERR_ARG;
     if (!s->pml_tab || !s->src || !s->state || !s->probe) return FDTDPIC_ERR_ARG;
     if (I.hist_rows > 0 && I.hist_interval > 0 && !s->hist) return FDTDPIC_ERR_ARG;
-    if (s->n_part < 0) return FDTDPIC_ERR_ARG;
+    if (s->n_part < 0 || s->n_part > FDTDPIC_MAX_PARTICLES) return FDTDPIC_ERR_ARG;
     if (s->n_part > 0) {
         if (s->clo < 2 || s->chi <= s->clo || s->chi > I.nz - 2) return FDTDPIC_ERR_ARG;
         if (!s->cell || !s->frac || !s->ux || !s->uz || !s->hyp || !s->jx || !s->jz || !s->acc)

@@ -51,3 +51,32 @@ def test_run_refuses_unknown_path_bits():
     # which also comes before any device work
     for path in (0, 1, 16, 16 | 1):
         assert run(path, 0) == -2, path
+
+
+def test_run_refuses_sizes_beyond_the_limits():
+    """FDTDPIC_MAX_PARTICLES and FDTDPIC_MAX_CELLS (2^30 each): larger beams and grids are
+    refused with FDTDPIC_ERR_ARG before any device work; at the limits the call gets on to the
+    scratch-size check."""
+    from fdtdpic import _lib
+    from fdtdpic.grid import lorentz_kerr_grid, pack
+    from fdtdpic.pic import PicBeam
+    L = _lib.lib()
+    g = lorentz_kerr_grid(512, 64, front=300, rear=400, nzsrc=60, probes=(50, 350))
+    desc = pack([g], 4)["desc"]
+    fake = ctypes.c_void_p(256)  # never dereferenced: every call below stops at a host check
+
+    def run(d, n_part):
+        pb = PicBeam()
+        pb.n_part, pb.clo, pb.chi, pb.sort_every = n_part, 40, 480, 32
+        pb.sc, pb.jscale, pb.path = 0.5, 1.0, 1
+        return L.fdtdpic_run(_lib.F32, d.ctypes.data, fake, fake, fake, fake, fake,
+                             ctypes.byref(pb), fake, fake, fake, fake, fake, fake, fake, fake,
+                             fake, 0, fake, None, None)
+
+    assert run(desc, (1 << 30) + 1) == -1
+    assert run(desc, 1 << 30) == -2
+    big = desc.copy()
+    big["nz"] = (1 << 30) + 1
+    assert run(big, 100) == -1
+    big["nz"] = 1 << 30
+    assert run(big, 100) == -2

@@ -40,6 +40,12 @@ def test_slot_check_accepts_and_rejects():
     s["probe"] = 0
     assert L.fdtdpic_slot_check(4, s.ctypes.data) != 0
     assert L.fdtdpic_slot_check(3, _slot().ctypes.data) != 0
+    # size limits (FDTDPIC_MAX_PARTICLES, FDTDPIC_MAX_CELLS = 2^30)
+    assert L.fdtdpic_slot_check(4, _slot(n_part=(1 << 30) + 1).ctypes.data) == -1
+    assert L.fdtdpic_slot_check(4, _slot(n_part=1 << 30).ctypes.data) == 0
+    s = _slot()
+    s["inst"]["nz"] = (1 << 30) + 1
+    assert L.fdtdpic_slot_check(4, s.ctypes.data) == -1
     # shared memory: field-only slots need their resident arrays, beam slots their accumulators
     assert L.fdtdpic_slot_smem_bytes(4, _slot(n_part=100).ctypes.data) == 2 * 301 * 8
     assert L.fdtdpic_slot_smem_bytes(8, _slot(n_part=100).ctypes.data) == 4 * 301 * 8
