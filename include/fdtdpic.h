@@ -272,6 +272,16 @@ int64_t fdtdpic_scratch_bytes(int precision, int nz, int n_part);
 int64_t fdtdpic_pic_scratch_bytes(int precision, const FdtdInstance *inst, const PicBeam *beam);
 /* The largest power-of-two scale for which no deposit accumulator can overflow. */
 double fdtdpic_pic_jscale(const PicBeam *beam);
+/* The tiling a temporally blocked run (PicBeam.path mode 3) takes on a device with smem_optin
+ * bytes of opt-in shared memory per CTA (cudaDevAttrMaxSharedMemoryPerBlockOptin; 232,448 on
+ * GB300), computed on the host for beam->sort_every and beam->chunk whatever beam->path holds.
+ * out (nullable, up to n_out values, in this order): steps a pass S, halo H = 3S+4 cells,
+ * tiles G, narrowest and widest tile, a tile's loaded range wmax + 2H, the particles one loaded
+ * range holds, shared memory of a one-tile CTA and of the CTA holding both wrap tiles, and
+ * fdtdpic_run's scratch bytes.  Returns the number of values (10) when the path applies, else
+ * FDTDPIC_ERR_ARG (the conditions at PicBeam.path). */
+int fdtdpic_pass_plan(int precision, const FdtdInstance *inst, const PicBeam *beam,
+                      int64_t smem_optin, int64_t *out, int n_out);
 
 /* Steps [step_begin, step_end) of one instance coupled to a beam.  Fields live in d_state (as
  * fdtd1d_run_global); d_hyp (nz+1) holds Hy one half step back (zero for a fresh run) and is

@@ -299,6 +299,25 @@ int64_t fdtdpic_pic_scratch_bytes(int precision, const FdtdInstance *inst, const
     return need;
 }
 
+int fdtdpic_pass_plan(int precision, const FdtdInstance *inst, const PicBeam *beam,
+                      int64_t smem_optin, int64_t *out, int n_out)
+{
+    if (!inst || !beam || (precision != FDTDPIC_F64 && precision != FDTDPIC_F32) || smem_optin < 0)
+        return FDTDPIC_ERR_ARG;
+    if (check_instance(*inst) != FDTDPIC_OK) return FDTDPIC_ERR_ARG;
+    const PicBeam &b = *beam;
+    if (b.n_part < 0 || b.n_part > FDTDPIC_MAX_PARTICLES || b.clo < 2 || b.chi <= b.clo ||
+        b.chi > inst->nz - 2 || b.sort_every < 0 || b.chunk < 0)
+        return FDTDPIC_ERR_ARG;
+    const PassGeom g = pass_geometry(precision, *inst, b, smem_optin);
+    if (!g.ok) return FDTDPIC_ERR_ARG;
+    const int64_t v[] = {g.S, g.H, g.G, g.wmin, g.wmax, g.Lmax, g.pcap, g.smem1, g.smem2,
+                         (int64_t)pass_scratch_layout(precision, inst->nz, g).total};
+    const int nv = (int)(sizeof(v) / sizeof(v[0]));
+    for (int i = 0; out && i < n_out && i < nv; ++i) out[i] = v[i];
+    return nv;
+}
+
 int fdtdpic_run(int precision, const FdtdInstance *h_inst, const FdtdInstance *d_inst,
                 const double *d_pml_tab, const double *d_src, void *d_state, void *d_probe,
                 const PicBeam *beam, int32_t *d_cell, void *d_frac, void *d_ux, void *d_uz,

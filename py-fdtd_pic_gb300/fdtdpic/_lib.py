@@ -187,6 +187,8 @@ def _declare(L):
     L.fdtdpic_run.argtypes = [c_int] + [P] * 16 + [c_i64, P, P, P]
     L.fdtdpic_pic_scratch_bytes.restype = c_i64
     L.fdtdpic_pic_scratch_bytes.argtypes = [c_int, P, P]
+    L.fdtdpic_pass_plan.restype = c_int
+    L.fdtdpic_pass_plan.argtypes = [c_int, P, P, c_i64, P, c_int]
     L.fdtdpic_dft_twiddle_bytes.restype = c_i64
     L.fdtdpic_dft_twiddle_bytes.argtypes = [c_int, c_int]
     L.fdtdpic_dft_twiddles.restype = c_int

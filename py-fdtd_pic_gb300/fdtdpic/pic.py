@@ -76,6 +76,29 @@ def beam_constants(dz, dt, weight, mu0, q=Q_E, m=M_E):
                 kJ=q * weight * C0, kJz=q * weight * dz / dt)
 
 
+PASS_PLAN_KEYS = ("steps", "halo", "tiles", "wmin", "wmax", "loaded", "particles_per_range",
+                  "smem_one_tile", "smem_wrap_pair", "scratch_bytes")
+
+
+def pass_plan(grid: Grid, beam: Beam, precision="f32", pass_steps=0, tile_cells=0,
+              smem_optin=232448):
+    """The tiling a ``PicRun(path="pass")`` takes, computed on the host for a device with
+    ``smem_optin`` bytes of opt-in shared memory per CTA (GB300: 232,448): a dict of
+    PASS_PLAN_KEYS, or None when the pass path does not apply (fdtdpic_pass_plan)."""
+    L = lib()
+    prec, _ = _dtype(precision)
+    desc = pack([grid], 8 if prec == F64 else 4)["desc"]
+    pb = PicBeam()
+    pb.n_part, pb.clo, pb.chi = beam.n, beam.clo, beam.chi
+    pb.sort_every, pb.chunk, pb.path = pass_steps, tile_cells, 3 | PATH_CELLS_INSIDE
+    out = (ctypes.c_int64 * len(PASS_PLAN_KEYS))()
+    n = L.fdtdpic_pass_plan(prec, desc.ctypes.data, ctypes.byref(pb), int(smem_optin), out,
+                            len(PASS_PLAN_KEYS))
+    if n < 0:
+        return None
+    return dict(zip(PASS_PLAN_KEYS, (int(v) for v in out[:n])))
+
+
 @dataclass
 class PicSnapshot:
     """Everything a :class:`PicRun` carries between calls, on the host (see PicRun.snapshot)."""

@@ -80,3 +80,40 @@ def test_run_refuses_sizes_beyond_the_limits():
     assert run(big, 100) == -1
     big["nz"] = 1 << 30
     assert run(big, 100) == -2
+
+
+def _plan(nz=8191, clo=40, chi=8189, ppc=4, **kw):
+    from fdtdpic.grid import lorentz_kerr_grid
+    from fdtdpic.pic import make_beam, pass_plan
+    g = lorentz_kerr_grid(nz, 64, front=nz // 4, rear=3 * nz // 4, nzsrc=60, probes=(50, nz // 2))
+    beam = make_beam(ppc * (chi - clo), clo, chi, 0.015)
+    return pass_plan(g, beam, **kw)
+
+
+def test_pass_plan_tiles_a_long_grid():
+    """fdtdpic_pass_plan on the host: 8192 nodes in 512-cell tiles, 8 steps a pass (halo
+    3 x 8 + 4 = 28 cells), the FP32 Kerr CTA holding both wrap tiles within GB300's 227 KiB of
+    shared memory; the defaults (0, 0) are 8 steps and 512 cells; longer passes are cut to 32."""
+    p = _plan(pass_steps=8, tile_cells=512)
+    assert p is not None
+    assert (p["steps"], p["halo"], p["tiles"], p["wmin"], p["wmax"]) == (8, 28, 16, 512, 512)
+    assert p["loaded"] == 512 + 2 * 28
+    assert p["particles_per_range"] >= 4 * p["loaded"]
+    assert 0 < p["smem_one_tile"] < p["smem_wrap_pair"] <= 232448 - 1024
+    assert p["scratch_bytes"] > 0
+    assert _plan() == p
+    assert _plan(pass_steps=64, tile_cells=512)["steps"] == 32
+
+
+def test_pass_plan_refusals():
+    """The conditions under which the pass path refuses a run, each alone."""
+    assert _plan(pass_steps=8, tile_cells=512) is not None
+    assert _plan(ppc=0) is None                                  # an empty beam
+    assert _plan(pass_steps=8, tile_cells=40) is None            # tiles narrower than 2H = 56
+    assert _plan(nz=2047, chi=2045) is None                      # four tiles: fewer than five
+    assert _plan(clo=500) is None                                # clo 12 cells from its tile's edge
+    assert _plan(chi=700) is None                                # the wrap tiles 2H apart at most
+    assert _plan(smem_optin=48 * 1024) is None                   # shared memory too small
+    # FP64 state and particles take twice the room: 256-cell tiles fit, 512-cell ones do not
+    assert _plan(precision="f64") is None
+    assert _plan(precision="f64", tile_cells=256) is not None
