@@ -109,7 +109,8 @@ def setup_records(n, *, dz, dt, courant, eps0, mu0, plasma_freq, omega0, gamma, 
 
 def run_setup(desc: np.ndarray, records: np.ndarray, device=None, stream=None):
     """Device copies of the descriptors with their coefficient fields filled, and the PML table
-    pool (pml_offset of each descriptor indexes it), from fdtdpic_setup_batch."""
+    pool (pml_offset of each descriptor indexes it), from fdtdpic_setup_batch enqueued on
+    ``stream`` (default: torch's current stream): they are ready on that stream."""
     _require_cuda()
     L = lib()
     dev = torch.device("cuda", torch.cuda.current_device()) if device is None else device

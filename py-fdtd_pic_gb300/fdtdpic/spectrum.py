@@ -43,23 +43,26 @@ def dft(traces, freqs, dt, stream=None) -> np.ndarray:
     if S == 0:
         out[:] = 0
         return out
-    d_x = x.cuda()
-    prec = 4 if d_x.dtype == torch.float32 else 8
     st = stream or torch.cuda.current_stream()
     sp = ctypes.c_void_p(st.cuda_stream)
-    per = max(1, min(F, _CHUNK_BYTES // (8 * S)))
-    d_tw = torch.empty(int(L.fdtdpic_dft_twiddle_bytes(per, S)), dtype=torch.uint8, device="cuda")
-    d_out = torch.empty(R * per * 2, dtype=torch.float64, device="cuda")
-    for f0 in range(0, F, per):
-        n = min(per, F - f0)
-        d_f = torch.from_numpy(freqs[f0:f0 + n].copy()).cuda()
-        check(L.fdtdpic_dft_twiddles(_ptr(d_f), n, S, float(dt), _ptr(d_tw), sp),
-              "fdtdpic_dft_twiddles")
-        # one trace per row: rp = 1, ldp = S, sp = 0, sn = 1
-        check(L.fdtdpic_dft_probes(prec, _ptr(d_x), R, S, 1, S, 0, 1, _ptr(d_tw), n,
-                                   _ptr(d_out), sp), "fdtdpic_dft_probes")
-        X = d_out[:R * n * 2].cpu().numpy().reshape(R, n, 2)
-        out[:, f0:f0 + n] = X[..., 0] + 1j * X[..., 1]
+    # copies, launches and the read-back all on st, in order
+    with torch.cuda.stream(st):
+        d_x = x.cuda()
+        prec = 4 if d_x.dtype == torch.float32 else 8
+        per = max(1, min(F, _CHUNK_BYTES // (8 * S)))
+        d_tw = torch.empty(int(L.fdtdpic_dft_twiddle_bytes(per, S)), dtype=torch.uint8,
+                           device="cuda")
+        d_out = torch.empty(R * per * 2, dtype=torch.float64, device="cuda")
+        for f0 in range(0, F, per):
+            n = min(per, F - f0)
+            d_f = torch.from_numpy(freqs[f0:f0 + n].copy()).cuda()
+            check(L.fdtdpic_dft_twiddles(_ptr(d_f), n, S, float(dt), _ptr(d_tw), sp),
+                  "fdtdpic_dft_twiddles")
+            # one trace per row: rp = 1, ldp = S, sp = 0, sn = 1
+            check(L.fdtdpic_dft_probes(prec, _ptr(d_x), R, S, 1, S, 0, 1, _ptr(d_tw), n,
+                                       _ptr(d_out), sp), "fdtdpic_dft_probes")
+            X = d_out[:R * n * 2].cpu().numpy().reshape(R, n, 2)
+            out[:, f0:f0 + n] = X[..., 0] + 1j * X[..., 1]
     return out
 
 

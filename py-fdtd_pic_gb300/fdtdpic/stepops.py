@@ -75,21 +75,23 @@ def run(op: FdtdStepOp, slots, writes, stream=None):
     bufs = {}
     ptrs = (ctypes.c_void_p * N_SLOTS)()
     dslot = [None] * N_SLOTS
-    for i, a in enumerate(slots):
-        if a is None:
-            continue
-        key = id(a)
-        if key not in bufs:
-            bufs[key] = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(dev)
-        dslot[i] = bufs[key]
-        ptrs[i] = bufs[key].data_ptr()
     st = stream or torch.cuda.current_stream()
-    check(L.fdtdpic_step_op(ctypes.byref(op), ptrs, n, ctypes.c_void_p(st.cuda_stream)),
-          "fdtdpic_step_op")
-    done = set()
-    for i in writes:
-        a = slots[i]
-        if a is None or id(a) in done:
-            continue
-        a[...] = dslot[i].cpu().numpy()
-        done.add(id(a))
+    # copies in, the launch and the copies back all on st, in order
+    with torch.cuda.stream(st):
+        for i, a in enumerate(slots):
+            if a is None:
+                continue
+            key = id(a)
+            if key not in bufs:
+                bufs[key] = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(dev)
+            dslot[i] = bufs[key]
+            ptrs[i] = bufs[key].data_ptr()
+        check(L.fdtdpic_step_op(ctypes.byref(op), ptrs, n, ctypes.c_void_p(st.cuda_stream)),
+              "fdtdpic_step_op")
+        done = set()
+        for i in writes:
+            a = slots[i]
+            if a is None or id(a) in done:
+                continue
+            a[...] = dslot[i].cpu().numpy()
+            done.add(id(a))
