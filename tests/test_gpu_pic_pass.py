@@ -126,3 +126,18 @@ def test_pass_path_long_grid_equals_streaming():
     want, got = out
     assert np.abs(want["jx"]).max() > 0
     _equal(got, want)
+
+
+@pytest.mark.parametrize("precision,tile", [("f32", 0), ("f64", 256)])
+def test_pass_plan_sizes_the_run(precision, tile):
+    """The host planner (fdtdpic_pass_plan at GB300's 227 KiB of opt-in shared memory) and a run
+    on this device take the same tiling: PicRun(path="pass") sizes the scratch the plan reports."""
+    _torch()
+    import scipy.constants as sc
+    from fdtdpic.pic import PicRun, make_beam, pass_plan
+    g = _grid("kerr")
+    beam = make_beam(NPART, CLO, CHI, DZ, v_spread=0.05)
+    plan = pass_plan(g, beam, precision=precision, tile_cells=tile)
+    assert plan is not None
+    run = PicRun(g, beam, DZ, DT, sc.mu_0, precision=precision, path="pass", tile_cells=tile)
+    assert run.scratch_bytes == plan["scratch_bytes"]
